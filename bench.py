@@ -1,0 +1,471 @@
+"""Benchmark of the scan / reduce hot path on GB300.
+
+Headline (one JSON line on rank 0): effective GB/s of the single-pass
+decoupled look-back inclusive plus-scan of n = 2^30 uint32 values drawn
+uniformly from [0, 2^16), counting 2n*4 bytes (read + write) per scan, with
+the input resident in HBM (4 GiB in + 4 GiB out, far above the 129 MB L2, so
+no flush is needed between steps). A step is one scan over the whole array.
+
+Also reported:
+  roofline      achieved GB/s of the scan kernel (CUDA events around every
+                launch on its stream) against the measured HBM copy peak;
+  e2e           the same metric through the blocking host-pointer C-ABI call
+                (pp_decoupled_scan_host): pinned host input -> device, scan,
+                device -> pinned host output, every step;
+  cpu_baseline  the reference's decoupled look-back algorithm restated in C
+                (oracle/oracle.c) on the host cores, on a bounded sample;
+  secondary     the other HBM-scale primitives of the same workload family.
+
+`--impl reference` times the reference's CPU algorithm alone (the oracle
+restatement, or the reference headers compiled against the SYCL CPU shim
+when that library exists for this machine) and prints its own line.
+
+Multi-GPU: the primitives do not shard in this library, so N > 1 runs N
+independent replicas (one per rank) and reports the total.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "sycl-building-blocks_gb300"
+ORACLE_DIR = ROOT / "oracle"
+sys.path.insert(0, str(PKG))
+
+N_HEADLINE = 1 << 30
+SEED = 0x5CA72026
+METRIC = "scan effective GB/s (2n bytes) vs HBM peak/memcpy; batched-segment elems/s"
+UNIT = "GB/s"
+
+
+def measured_peak() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel_key: str) -> float | None:
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    p = ROOT / "profiles" / "traffic.json"
+    try:
+        return float(json.loads(p.read_text())[kernel_key])
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the timed region runs."""
+
+    QUERY = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def barrier(torch):
+    if torch.distributed.is_available() and torch.distributed.is_initialized():
+        torch.distributed.barrier()
+
+
+def max_over_ranks(torch, v: float) -> float:
+    if torch.distributed.is_available() and torch.distributed.is_initialized():
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+    return v
+
+
+# ---------------------------------------------------------------------------------
+def time_device(torch, fn, steps: int, warmup: int, stream) -> tuple[float, list[float]]:
+    """Run fn() warmup + steps times on `stream`; return (total ms of the timed
+    steps bracketed by barrier + synchronize, per-launch ms from events)."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    barrier(torch)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for a, b in evs:
+        a.record(stream)
+        fn()
+        b.record(stream)
+    end.record(stream)
+    torch.cuda.synchronize()
+    barrier(torch)
+    torch.cuda.synchronize()
+    return start.elapsed_time(end), [a.elapsed_time(b) for a, b in evs]
+
+
+def run_ours(args) -> dict | None:
+    import numpy as np
+    import torch
+
+    import ppbuild
+
+    ws, rank, local = dist_info()
+    if ws > 1 and not torch.distributed.is_initialized():
+        torch.distributed.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    ppbuild.build()
+    import ppgb300 as pp
+
+    pp.lib()
+    n = args.n
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    # input: seeded U[0, 2^16) uint32 generated on the device (torch's Philox)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(SEED + rank)
+    d_in = torch.randint(0, 1 << 16, (n,), dtype=torch.int32, device="cuda", generator=gen)
+    d_out = torch.empty_like(d_in)
+    algo_bytes = 2 * n * 4
+
+    def step():
+        pp.decoupled_scan_device("inclusive", "plus", d_in.data_ptr(), d_out.data_ptr(), n, "u32", stream=sh)
+
+    step()
+    if pp.stream_status(sh) != 0:
+        raise RuntimeError("device error in warm-up scan")
+    # sanity: last prefix == total (mod 2^32), first == in[0]
+    total = int(d_in.to(torch.int64).sum().item()) & 0xFFFFFFFF
+    verified = (int(d_out[-1].item()) & 0xFFFFFFFF) == total and int(d_out[0].item()) == int(d_in[0].item())
+
+    gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0] or 0) if \
+        os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else local
+    sampler = ClockSampler(gpu_index)
+    sampler.start()
+    time.sleep(0.2)
+    total_ms, per_launch = time_device(torch, step, args.steps, args.warmup, stream)
+    clocks = sampler.stop()
+    if pp.stream_status(sh) != 0:
+        raise RuntimeError("device error during the timed scans")
+    total_ms = max_over_ranks(torch, total_ms)
+    ms_per_step = total_ms / args.steps
+    value = ws * algo_bytes * args.steps / (total_ms * 1e-3) / 1e9
+    launch_ms = statistics.mean(per_launch)
+    achieved = algo_bytes / (launch_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak()
+
+    # device-to-device copy of the same bytes, re-measured in this run
+    def copy_step():
+        d_out.copy_(d_in)
+
+    cp_ms, _ = time_device(torch, copy_step, max(3, args.steps // 4), 2, stream)
+    memcpy_gbs = algo_bytes * max(3, args.steps // 4) / (cp_ms * 1e-3) / 1e9
+
+    secondary = {} if args.no_secondary else run_secondary(torch, pp, stream, args, d_in, d_out)
+
+    # end to end through the host-pointer C-ABI call
+    e2e_steps = max(2, min(args.steps, args.e2e_steps))
+    h_in = torch.empty(n, dtype=torch.int32, pin_memory=True)
+    h_out = torch.empty(n, dtype=torch.int32, pin_memory=True)
+    h_in.copy_(d_in)
+    torch.cuda.synchronize()
+    L = pp.lib()
+
+    def e2e_step():
+        st = L.pp_decoupled_scan_host(0, 0, 1, h_in.data_ptr(), h_out.data_ptr(), n)
+        if st != 0:
+            raise RuntimeError(f"pp_decoupled_scan_host failed: {st}")
+
+    e2e_step()
+    barrier(torch)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier(torch)
+    e2e_s = max_over_ranks(torch, time.perf_counter() - t0)
+    e2e_value = ws * algo_bytes * e2e_steps / e2e_s / 1e9
+    e2e_ok = bool(np.array_equal(h_out[-4:].numpy(), d_out[-4:].cpu().numpy()))
+    del h_in, h_out
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(d_in, args)
+
+    if rank != 0:
+        return None
+    traffic = ncu_traffic("decoupled_scan_u32_2p30")
+    return {
+        "metric": METRIC,
+        "value": round(value, 2),
+        "unit": UNIT,
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_per_step, 5),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u32",
+        "data": "synthetic: seeded uniform [0, 2^16) uint32 generated on the device",
+        "config": {
+            "workload": "decoupled look-back inclusive plus-scan, n=2^30 uint32 U[0,2^16)",
+            "n": n,
+            "bytes_per_step": algo_bytes,
+            "l2": "inputs (4 GiB) larger than L2 (129 MB); no flush",
+            "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+            "verified_last_prefix": verified,
+        },
+        "roofline": {
+            "bound": "hbm",
+            "achieved": round(achieved, 2),
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": round(achieved / peak, 4),
+            "peak_kind": peak_kind,
+            "traffic": traffic,
+            "memcpy_gbs_this_run": round(memcpy_gbs, 2),
+            "frac_of_memcpy_this_run": round(achieved / memcpy_gbs, 4),
+        },
+        "e2e": {
+            "value": round(e2e_value, 2),
+            "unit": UNIT,
+            "h2d_bytes_per_step": n * 4,
+            "d2h_bytes_per_step": n * 4,
+            "api": "pp_decoupled_scan_host (pinned host buffers)",
+            "verified_tail": e2e_ok,
+        },
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+        "secondary": secondary,
+    }
+
+
+def run_secondary(torch, pp, stream, args, d_in32, d_out32) -> dict:
+    """The other HBM-scale configurations: GB/s of each at 2n (scan) or n (reduce) bytes."""
+    out = {}
+    sh = stream.cuda_stream
+    n30 = args.n
+    steps = max(3, args.steps // 5)
+
+    def rate(fn, nbytes):
+        ms, per = time_device(torch, fn, steps, 2, stream)
+        if pp.stream_status(sh) != 0:
+            raise RuntimeError("device error in secondary benchmark")
+        return round(nbytes * steps / (ms * 1e-3) / 1e9, 2)
+
+    out["u32_exclusive_plus_2p30"] = rate(
+        lambda: pp.decoupled_scan_device("exclusive", "plus", d_in32.data_ptr(), d_out32.data_ptr(), n30, "u32",
+                                         stream=sh), 8 * n30)
+    out["u32_cooperative_inclusive_plus_2p30"] = rate(
+        lambda: pp.cooperative_scan_device("inclusive", "plus", d_in32.data_ptr(), d_out32.data_ptr(), n30, "u32",
+                                           stream=sh), 8 * n30)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(SEED + 1)
+    full = torch.randint(-(1 << 31), (1 << 31) - 1, (n30,), dtype=torch.int32, device="cuda", generator=gen)
+    out["i32_max_scan_2p30"] = rate(
+        lambda: pp.decoupled_scan_device("inclusive", "maximum", full.data_ptr(), d_out32.data_ptr(), n30, "i32",
+                                         stream=sh), 8 * n30)
+    del full
+    n28 = args.n // 4
+    u64 = torch.randint(0, 1 << 32, (n28,), dtype=torch.int64, device="cuda", generator=gen)
+    o64 = torch.empty_like(u64)
+    for kind in ("inclusive", "exclusive"):
+        out[f"u64_{kind}_plus_2p28"] = rate(
+            lambda k=kind: pp.decoupled_scan_device(k, "plus", u64.data_ptr(), o64.data_ptr(), n28, "u64", stream=sh),
+            16 * n28)
+    del u64, o64
+    f = torch.randn(n30, dtype=torch.float32, device="cuda", generator=gen)
+    res = torch.empty(2, dtype=torch.float32, device="cuda")
+    out["f32_sum_reduce_2p30"] = rate(
+        lambda: pp.reduce("plus", f.data_ptr(), n30, "f32", res.data_ptr(), stream=sh), 4 * n30)
+    out["f32_max_reduce_2p30"] = rate(
+        lambda: pp.reduce("maximum", f.data_ptr(), n30, "f32", res.data_ptr() + 4, stream=sh), 4 * n30)
+    r = res.cpu().numpy()
+    ref_sum = float(f.double().sum().item())
+    ref_max = float(f.max().item())
+    out["f32_reduce_check"] = {"sum": float(r[0]), "fp64_sum": ref_sum, "abs_err": abs(float(r[0]) - ref_sum),
+                               "max_exact": float(r[1]) == ref_max}
+    del f
+    return out
+
+
+# ---------------------------------------------------------------------------------
+def load_cpu_reference():
+    """The reference's CPU code: the headers compiled against the SYCL shim
+    when that library exists for this machine, else the C restatement."""
+    sys.path.insert(0, str(ORACLE_DIR))
+    import pyoracle
+
+    pyoracle.lib()
+    ref = ORACLE_DIR / "_ref" / "libsyclref.so"
+    if ref.exists():
+        try:
+            import ctypes
+
+            lib = ctypes.CDLL(str(ref))
+            lib.ref_decoupled_scan_u32_plus.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                                         ctypes.c_int]
+            lib.ref_decoupled_scan_u32_plus.restype = ctypes.c_int
+            lib.ref_num_groups.restype = ctypes.c_int
+
+            def run(a, out):
+                if lib.ref_decoupled_scan_u32_plus(a.ctypes.data, out.ctypes.data, a.size, 0) != 0:
+                    raise RuntimeError("reference decoupled scan failed")
+
+            return "reference", run, int(lib.ref_num_groups()), pyoracle
+        except (OSError, AttributeError):
+            pass
+
+    def run(a, out):
+        pyoracle.ref_decoupled_scan(a, "plus", False, threads=0, out=out)
+
+    return "port", run, pyoracle.num_threads(), pyoracle
+
+
+def cpu_baseline(d_in, args) -> dict:
+    import numpy as np
+
+    kind, run, cores, pyoracle = load_cpu_reference()
+    m = min(args.cpu_sample, d_in.numel())
+    a = d_in[:m].cpu().numpy().view(np.uint32).copy()
+    out = np.empty_like(a)
+    run(a, out)  # warm
+    ok = bool(np.array_equal(out, pyoracle.scan(a, "plus")))
+    reps, t_total = 0, 0.0
+    while (t_total < args.cpu_seconds and reps < 200) or reps < 2:
+        t0 = time.perf_counter()
+        run(a, out)
+        t_total += time.perf_counter() - t0
+        reps += 1
+    gbs = 2 * m * 4 * reps / t_total / 1e9
+    return {"value": round(gbs, 3), "unit": UNIT, "cores": cores, "kind": kind,
+            "sample": f"first {m} elements of the same input, {reps} repetitions, {t_total:.1f} s",
+            "matches_oracle": ok}
+
+
+def run_reference(args) -> dict | None:
+    import numpy as np
+
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return None
+    kind, run, cores, pyoracle = load_cpu_reference()
+    m = min(args.cpu_sample, args.n)
+    a = pyoracle.gen_u32(SEED, m, 0, 1 << 16)
+    out = np.empty_like(a)
+    for _ in range(args.warmup):
+        run(a, out)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        run(a, out)
+    dt = time.perf_counter() - t0
+    ok = bool(np.array_equal(out, pyoracle.scan(a, "plus")))
+    value = 2 * m * 4 * args.steps / dt / 1e9
+    return {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": round(value, 3),
+        "unit": UNIT,
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(dt * 1e3 / args.steps, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u32",
+        "data": "synthetic: seeded uniform [0, 2^16) uint32 (splitmix64)",
+        "config": {
+            "workload": "decoupled look-back inclusive plus-scan, n=2^30 uint32 U[0,2^16)",
+            "n": args.n,
+            "sample_per_step": m,
+        },
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": f"{m} of the {args.n} elements per step", "matches_oracle": ok},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=N_HEADLINE)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-sample", type=int, default=1 << 26)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    res = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

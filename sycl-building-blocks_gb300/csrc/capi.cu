@@ -1,0 +1,334 @@
+// extern "C" entry points of libppgb300.so (declared in include/pp_gb300.h).
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+
+#include <cuda_runtime.h>
+
+#include "dispatch.cuh"
+
+using pp::capi::ScanReq;
+using pp::host::Status;
+
+namespace {
+
+pp_status to_c(Status s) { return static_cast<pp_status>(static_cast<int>(s)); }
+
+bool valid_kind(pp_scan_kind k) { return k == PP_SCAN_INCLUSIVE || k == PP_SCAN_EXCLUSIVE; }
+bool valid_op(pp_op op) { return op >= PP_OP_PLUS && op <= PP_OP_MAXIMUM; }
+bool valid_dtype(pp_dtype d) { return d >= PP_I32 && d <= PP_F64; }
+bool valid_algo(pp_scan_algo a) { return a >= PP_ALGO_AUTO && a <= PP_ALGO_SINGLE_GROUP; }
+bool valid_prec(pp_precision p) { return p >= PP_PREC_DEFAULT && p <= PP_PREC_FP64_CARRY; }
+bool is_float(pp_dtype d) { return d == PP_F32 || d == PP_F64; }
+bool is_bitop(pp_op op) { return op == PP_OP_BIT_AND || op == PP_OP_BIT_OR || op == PP_OP_BIT_XOR; }
+
+size_t dtype_size(pp_dtype d) {
+  switch (d) {
+    case PP_I32:
+    case PP_U32:
+    case PP_F32:
+      return 4;
+    default:
+      return 8;
+  }
+}
+
+// Validation that needs no GPU: enums, pointers, combinations.
+pp_status check_scan_args(pp_scan_kind kind, pp_op op, pp_dtype dt, const void* in, const void* out, uint64_t n,
+                          pp_scan_algo algo, pp_precision prec) {
+  if (!valid_kind(kind) || !valid_op(op) || !valid_dtype(dt) || !valid_algo(algo) || !valid_prec(prec))
+    return PP_ERR_INVALID_ARG;
+  if (n > 0 && (!in || !out)) return PP_ERR_INVALID_ARG;
+  if (is_float(dt) && is_bitop(op)) return PP_ERR_UNSUPPORTED;
+  if (prec != PP_PREC_DEFAULT && (dt != PP_F32 || op != PP_OP_PLUS)) return PP_ERR_UNSUPPORTED;
+  return PP_OK;
+}
+
+Status scan_dispatch(const ScanReq& r, pp_dtype dt, pp_precision prec) {
+  using namespace pp::capi;
+  if (prec != PP_PREC_DEFAULT) return scan_f32_precision(r, prec);
+  switch (dt) {
+    case PP_I32:
+      return scan_typed<int32_t>(r);
+    case PP_U32:
+      return scan_typed<uint32_t>(r);
+    case PP_I64:
+      return scan_typed<int64_t>(r);
+    case PP_U64:
+      return scan_typed<uint64_t>(r);
+    case PP_F32:
+      return scan_typed<float>(r);
+    case PP_F64:
+      return scan_typed<double>(r);
+  }
+  return Status::invalid_arg;
+}
+
+Status reduce_dispatch(cudaStream_t s, pp_op op, pp_dtype dt, const void* in, uint64_t n, void* d_res, void* ws,
+                       size_t ws_bytes) {
+  using namespace pp::capi;
+  switch (dt) {
+    case PP_I32:
+      return reduce_typed<int32_t>(s, op, in, n, d_res, ws, ws_bytes);
+    case PP_U32:
+      return reduce_typed<uint32_t>(s, op, in, n, d_res, ws, ws_bytes);
+    case PP_I64:
+      return reduce_typed<int64_t>(s, op, in, n, d_res, ws, ws_bytes);
+    case PP_U64:
+      return reduce_typed<uint64_t>(s, op, in, n, d_res, ws, ws_bytes);
+    case PP_F32:
+      return reduce_typed<float>(s, op, in, n, d_res, ws, ws_bytes);
+    case PP_F64:
+      return reduce_typed<double>(s, op, in, n, d_res, ws, ws_bytes);
+  }
+  return Status::invalid_arg;
+}
+
+pp_status scan_entry(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dt, const void* in, void* out,
+                     uint64_t n, pp_scan_algo algo, pp_precision prec, void* ws, size_t ws_bytes) {
+  pp_status c = check_scan_args(kind, op, dt, in, out, n, algo, prec);
+  if (c != PP_OK) return c;
+  if (n == 0) return PP_OK;
+  ScanReq r;
+  r.s = static_cast<cudaStream_t>(stream);
+  r.exclusive = kind == PP_SCAN_EXCLUSIVE;
+  r.op = op;
+  r.in = in;
+  r.out = out;
+  r.n = n;
+  r.algo = algo;
+  r.ws = ws;
+  r.ws_bytes = ws_bytes;
+  return to_c(scan_dispatch(r, dt, prec));
+}
+
+// Device buffers reused by the blocking host-pointer wrappers.
+struct HostStaging {
+  std::mutex mu;
+  void* d_in = nullptr;
+  void* d_out = nullptr;
+  size_t bytes = 0;
+  int device = -1;
+};
+HostStaging& staging() {
+  static HostStaging* s = new HostStaging();
+  return *s;
+}
+
+pp_status ensure_staging(HostStaging& st, size_t bytes) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return PP_ERR_NO_DEVICE;
+  if (st.device == dev && st.bytes >= bytes) return PP_OK;
+  if (st.d_in) cudaFree(st.d_in);
+  if (st.d_out) cudaFree(st.d_out);
+  st.d_in = st.d_out = nullptr;
+  st.bytes = 0;
+  if (cudaMalloc(&st.d_in, bytes) != cudaSuccess) return PP_ERR_CUDA;
+  if (cudaMalloc(&st.d_out, bytes) != cudaSuccess) {
+    cudaFree(st.d_in);
+    st.d_in = nullptr;
+    return PP_ERR_CUDA;
+  }
+  st.bytes = bytes;
+  st.device = dev;
+  return PP_OK;
+}
+
+pp_status host_scan_entry(pp_scan_kind kind, pp_op op, pp_dtype dt, const void* h_in, void* h_out, uint64_t n,
+                          pp_scan_algo algo) {
+  pp_status c = check_scan_args(kind, op, dt, h_in, h_out, n, algo, PP_PREC_DEFAULT);
+  if (c != PP_OK) return c;
+  if (n == 0) return PP_OK;
+  const size_t bytes = n * dtype_size(dt);
+  HostStaging& st = staging();
+  std::lock_guard<std::mutex> g(st.mu);
+  c = ensure_staging(st, bytes);
+  if (c != PP_OK) return c;
+  cudaStream_t s = nullptr;
+  if (cudaMemcpyAsync(st.d_in, h_in, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return PP_ERR_CUDA;
+  c = scan_entry(s, kind, op, dt, st.d_in, st.d_out, n, algo, PP_PREC_DEFAULT, nullptr, 0);
+  if (c != PP_OK) return c;
+  if (cudaMemcpyAsync(h_out, st.d_out, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess) return PP_ERR_CUDA;
+  return to_c(pp::host::read_device_error(s, nullptr));
+}
+
+}  // namespace
+
+extern "C" {
+
+pp_status pp_scan(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dtype, const void* d_in, void* d_out,
+                  uint64_t n, pp_scan_algo algo, pp_precision precision) {
+  return scan_entry(stream, kind, op, dtype, d_in, d_out, n, algo, precision, nullptr, 0);
+}
+
+pp_status pp_scan_ws(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dtype, const void* d_in, void* d_out,
+                     uint64_t n, pp_scan_algo algo, pp_precision precision, void* d_workspace,
+                     size_t workspace_bytes) {
+  if (!d_workspace) return PP_ERR_INVALID_ARG;
+  return scan_entry(stream, kind, op, dtype, d_in, d_out, n, algo, precision, d_workspace, workspace_bytes);
+}
+
+pp_status pp_workspace_size(pp_scan_algo algo, pp_dtype dtype, pp_precision precision, const void* d_in,
+                            const void* d_out, uint64_t n, size_t* bytes) {
+  if (!bytes || !valid_algo(algo) || !valid_dtype(dtype) || !valid_prec(precision)) return PP_ERR_INVALID_ARG;
+  using namespace pp::capi;
+  if (precision != PP_PREC_DEFAULT) {
+    if (dtype != PP_F32) return PP_ERR_UNSUPPORTED;
+    *bytes = workspace_f32_precision(algo, precision, d_in, d_out, n);
+    return PP_OK;
+  }
+  switch (dtype) {
+    case PP_I32:
+      *bytes = workspace_typed<int32_t>(algo, d_in, d_out, n);
+      break;
+    case PP_U32:
+      *bytes = workspace_typed<uint32_t>(algo, d_in, d_out, n);
+      break;
+    case PP_I64:
+      *bytes = workspace_typed<int64_t>(algo, d_in, d_out, n);
+      break;
+    case PP_U64:
+      *bytes = workspace_typed<uint64_t>(algo, d_in, d_out, n);
+      break;
+    case PP_F32:
+      *bytes = workspace_typed<float>(algo, d_in, d_out, n);
+      break;
+    case PP_F64:
+      *bytes = workspace_typed<double>(algo, d_in, d_out, n);
+      break;
+  }
+  return PP_OK;
+}
+
+pp_status pp_decoupled_scan_device(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dtype,
+                                   const void* d_in, void* d_out, uint64_t n) {
+  return pp_scan(stream, kind, op, dtype, d_in, d_out, n, PP_ALGO_DECOUPLED, PP_PREC_DEFAULT);
+}
+
+pp_status pp_cooperative_scan_device(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dtype,
+                                     const void* d_in, void* d_out, uint64_t n) {
+  return pp_scan(stream, kind, op, dtype, d_in, d_out, n, PP_ALGO_COOPERATIVE, PP_PREC_DEFAULT);
+}
+
+pp_status pp_scan_device(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dtype, const void* d_in,
+                         void* d_out, uint64_t n) {
+  return pp_scan(stream, kind, op, dtype, d_in, d_out, n, PP_ALGO_DECOUPLED, PP_PREC_DEFAULT);
+}
+
+pp_status pp_group_scan_device(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dtype, const void* d_in,
+                               void* d_out, uint64_t n) {
+  return pp_scan(stream, kind, op, dtype, d_in, d_out, n, PP_ALGO_SINGLE_GROUP, PP_PREC_DEFAULT);
+}
+
+pp_status pp_reduce(pp_stream stream, pp_op op, pp_dtype dtype, const void* d_in, uint64_t n, void* d_result) {
+  if (!valid_op(op) || !valid_dtype(dtype) || !d_result || (n > 0 && !d_in)) return PP_ERR_INVALID_ARG;
+  if (is_float(dtype) && is_bitop(op)) return PP_ERR_UNSUPPORTED;
+  return to_c(reduce_dispatch(static_cast<cudaStream_t>(stream), op, dtype, d_in, n, d_result, nullptr, 0));
+}
+
+pp_status pp_reduce_ws(pp_stream stream, pp_op op, pp_dtype dtype, const void* d_in, uint64_t n, void* d_result,
+                       void* d_workspace, size_t workspace_bytes) {
+  if (!valid_op(op) || !valid_dtype(dtype) || !d_result || !d_workspace || (n > 0 && !d_in))
+    return PP_ERR_INVALID_ARG;
+  if (is_float(dtype) && is_bitop(op)) return PP_ERR_UNSUPPORTED;
+  return to_c(reduce_dispatch(static_cast<cudaStream_t>(stream), op, dtype, d_in, n, d_result, d_workspace,
+                              workspace_bytes));
+}
+
+pp_status pp_reduce_device(pp_stream stream, pp_op op, pp_dtype dtype, const void* d_in, uint64_t n,
+                           void* h_result) {
+  if (!h_result) return PP_ERR_INVALID_ARG;
+  if (!valid_op(op) || !valid_dtype(dtype) || (n > 0 && !d_in)) return PP_ERR_INVALID_ARG;
+  if (is_float(dtype) && is_bitop(op)) return PP_ERR_UNSUPPORTED;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  HostStaging& st = staging();
+  std::lock_guard<std::mutex> g(st.mu);
+  pp_status c = ensure_staging(st, 16);
+  if (c != PP_OK) return c;
+  Status r = reduce_dispatch(s, op, dtype, d_in, n, st.d_out, nullptr, 0);
+  if (r != Status::ok) return to_c(r);
+  if (cudaMemcpyAsync(h_result, st.d_out, dtype_size(dtype), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return PP_ERR_CUDA;
+  return to_c(pp::host::read_device_error(s, nullptr));
+}
+
+pp_status pp_decoupled_scan_host(pp_scan_kind kind, pp_op op, pp_dtype dtype, const void* h_in, void* h_out,
+                                 uint64_t n) {
+  return host_scan_entry(kind, op, dtype, h_in, h_out, n, PP_ALGO_DECOUPLED);
+}
+pp_status pp_cooperative_scan_host(pp_scan_kind kind, pp_op op, pp_dtype dtype, const void* h_in, void* h_out,
+                                   uint64_t n) {
+  return host_scan_entry(kind, op, dtype, h_in, h_out, n, PP_ALGO_COOPERATIVE);
+}
+pp_status pp_scan_host(pp_scan_kind kind, pp_op op, pp_dtype dtype, const void* h_in, void* h_out, uint64_t n) {
+  return host_scan_entry(kind, op, dtype, h_in, h_out, n, PP_ALGO_DECOUPLED);
+}
+
+pp_status pp_reduce_host(pp_op op, pp_dtype dtype, const void* h_in, uint64_t n, void* h_result) {
+  if (!h_result || !valid_op(op) || !valid_dtype(dtype) || (n > 0 && !h_in)) return PP_ERR_INVALID_ARG;
+  if (is_float(dtype) && is_bitop(op)) return PP_ERR_UNSUPPORTED;
+  const size_t bytes = n * dtype_size(dtype);
+  HostStaging& st = staging();
+  std::lock_guard<std::mutex> g(st.mu);
+  pp_status c = ensure_staging(st, bytes < 16 ? 16 : bytes);
+  if (c != PP_OK) return c;
+  cudaStream_t s = nullptr;
+  if (bytes && cudaMemcpyAsync(st.d_in, h_in, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return PP_ERR_CUDA;
+  Status r = reduce_dispatch(s, op, dtype, st.d_in, n, st.d_out, nullptr, 0);
+  if (r != Status::ok) return to_c(r);
+  if (cudaMemcpyAsync(h_result, st.d_out, dtype_size(dtype), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return PP_ERR_CUDA;
+  return to_c(pp::host::read_device_error(s, nullptr));
+}
+
+const char* pp_status_string(pp_status status) {
+  switch (status) {
+    case PP_OK:
+      return "ok";
+    case PP_ERR_INVALID_ARG:
+      return "invalid argument";
+    case PP_ERR_UNSUPPORTED:
+      return "unsupported operator / type / precision combination";
+    case PP_ERR_GRID_TOO_LARGE:
+      return "cooperative grid larger than the device can hold co-resident";
+    case PP_ERR_TIMEOUT:
+      return "a device-side wait timed out";
+    case PP_ERR_CUDA:
+      return "CUDA runtime error";
+    case PP_ERR_WORKSPACE:
+      return "workspace too small (or allocation needed during stream capture)";
+    case PP_ERR_NO_DEVICE:
+      return "no usable CUDA device";
+  }
+  return "unknown status";
+}
+
+pp_status pp_stream_status(pp_stream stream) {
+  return to_c(pp::host::read_device_error(static_cast<cudaStream_t>(stream), nullptr));
+}
+
+pp_status pp_workspace_status(pp_stream stream, void* d_workspace) {
+  if (!d_workspace) return PP_ERR_INVALID_ARG;
+  return to_c(pp::host::read_device_error(static_cast<cudaStream_t>(stream), d_workspace));
+}
+
+pp_status pp_set_timeout_ns(uint64_t ns) {
+  if (ns == 0) return PP_ERR_INVALID_ARG;
+  pp::host::settings().timeout_ns.store(ns);
+  return PP_OK;
+}
+
+pp_status pp_set_max_ctas(int ctas) {
+  if (ctas < 0) return PP_ERR_INVALID_ARG;
+  pp::host::settings().max_ctas.store(ctas);
+  return PP_OK;
+}
+
+pp_status pp_debug_set_skip_tile(long long tile) {
+  pp::host::settings().debug_skip_tile.store(tile < 0 ? -1 : tile);
+  return PP_OK;
+}
+
+const char* pp_version(void) { return "ppgb300 0.1.0 (sm_103a)"; }
+
+}  // extern "C"

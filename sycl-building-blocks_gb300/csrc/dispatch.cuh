@@ -1,0 +1,45 @@
+// Run-time dispatch from the C ABI enums to the kernel templates. The typed
+// entry points are defined in dispatch_impl.cuh and explicitly instantiated
+// once per element type in capi_<type>.cu, so the instantiations compile in
+// parallel translation units.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "pp/host.cuh"
+#include "pp_gb300.h"
+
+namespace pp {
+namespace capi {
+
+using host::Status;
+
+struct ScanReq {
+  cudaStream_t s = nullptr;
+  bool exclusive = false;
+  pp_op op = PP_OP_PLUS;
+  const void* in = nullptr;
+  void* out = nullptr;
+  uint64_t n = 0;
+  pp_scan_algo algo = PP_ALGO_AUTO;
+  void* ws = nullptr;
+  size_t ws_bytes = 0;
+};
+
+template <class T>
+Status scan_typed(const ScanReq& r);
+template <class T>
+Status reduce_typed(cudaStream_t s, pp_op op, const void* in, uint64_t n, void* d_result, void* ws,
+                    size_t ws_bytes);
+template <class T>
+size_t workspace_typed(pp_scan_algo algo, const void* in, const void* out, uint64_t n);
+
+// F32 plus-scan with a precision mode (capi_precision.cu).
+Status scan_f32_precision(const ScanReq& r, pp_precision prec);
+size_t workspace_f32_precision(pp_scan_algo algo, pp_precision prec, const void* in, const void* out, uint64_t n);
+
+}  // namespace capi
+}  // namespace pp

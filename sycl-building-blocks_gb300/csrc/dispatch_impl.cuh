@@ -1,0 +1,95 @@
+// Definitions of the typed dispatch functions declared in dispatch.cuh.
+#pragma once
+
+#include <type_traits>
+
+#include "dispatch.cuh"
+
+namespace pp {
+namespace capi {
+
+template <class Pol>
+Status scan_policy(const ScanReq& r) {
+  switch (r.algo) {
+    case PP_ALGO_AUTO:
+    case PP_ALGO_DECOUPLED:
+      return host::decoupled_scan<Pol>(r.s, r.in, r.out, r.n, r.exclusive, r.ws, r.ws_bytes, 0);
+    case PP_ALGO_SINGLE_GROUP:
+      return host::decoupled_scan<Pol>(r.s, r.in, r.out, r.n, r.exclusive, r.ws, r.ws_bytes, 1);
+    case PP_ALGO_COOPERATIVE:
+      return host::cooperative_scan<Pol>(r.s, r.in, r.out, r.n, r.exclusive, r.ws, r.ws_bytes, 0);
+  }
+  return Status::invalid_arg;
+}
+
+template <class Pol>
+size_t workspace_policy(pp_scan_algo algo, const void* in, const void* out, uint64_t n) {
+  if (algo == PP_ALGO_COOPERATIVE) return workspace_bytes_for_desc_words(0);
+  return host::decoupled_workspace_bytes<Pol>(n, in, out);
+}
+
+template <class T>
+Status scan_typed(const ScanReq& r) {
+  switch (r.op) {
+    case PP_OP_PLUS:
+      return scan_policy<PlainScan<T, plus>>(r);
+    case PP_OP_MULTIPLIES:
+      return scan_policy<PlainScan<T, multiplies>>(r);
+    case PP_OP_MINIMUM:
+      return scan_policy<PlainScan<T, minimum>>(r);
+    case PP_OP_MAXIMUM:
+      return scan_policy<PlainScan<T, maximum>>(r);
+    case PP_OP_BIT_AND:
+    case PP_OP_BIT_OR:
+    case PP_OP_BIT_XOR:
+      if constexpr (std::is_integral_v<T>) {
+        if (r.op == PP_OP_BIT_AND) return scan_policy<PlainScan<T, bit_and>>(r);
+        if (r.op == PP_OP_BIT_OR) return scan_policy<PlainScan<T, bit_or>>(r);
+        return scan_policy<PlainScan<T, bit_xor>>(r);
+      } else {
+        return Status::unsupported;
+      }
+  }
+  return Status::invalid_arg;
+}
+
+template <class T>
+Status reduce_typed(cudaStream_t s, pp_op op, const void* in, uint64_t n, void* d_result, void* ws,
+                    size_t ws_bytes) {
+  const T* p = static_cast<const T*>(in);
+  T* res = static_cast<T*>(d_result);
+  switch (op) {
+    case PP_OP_PLUS:
+      return host::reduce<T, plus>(s, p, n, res, ws, ws_bytes);
+    case PP_OP_MULTIPLIES:
+      return host::reduce<T, multiplies>(s, p, n, res, ws, ws_bytes);
+    case PP_OP_MINIMUM:
+      return host::reduce<T, minimum>(s, p, n, res, ws, ws_bytes);
+    case PP_OP_MAXIMUM:
+      return host::reduce<T, maximum>(s, p, n, res, ws, ws_bytes);
+    case PP_OP_BIT_AND:
+    case PP_OP_BIT_OR:
+    case PP_OP_BIT_XOR:
+      if constexpr (std::is_integral_v<T>) {
+        if (op == PP_OP_BIT_AND) return host::reduce<T, bit_and>(s, p, n, res, ws, ws_bytes);
+        if (op == PP_OP_BIT_OR) return host::reduce<T, bit_or>(s, p, n, res, ws, ws_bytes);
+        return host::reduce<T, bit_xor>(s, p, n, res, ws, ws_bytes);
+      } else {
+        return Status::unsupported;
+      }
+  }
+  return Status::invalid_arg;
+}
+
+template <class T>
+size_t workspace_typed(pp_scan_algo algo, const void* in, const void* out, uint64_t n) {
+  return workspace_policy<PlainScan<T, plus>>(algo, in, out, n);
+}
+
+#define PP_INSTANTIATE_DISPATCH(T)                                                                     \
+  template Status scan_typed<T>(const ScanReq&);                                                       \
+  template Status reduce_typed<T>(cudaStream_t, pp_op, const void*, uint64_t, void*, void*, size_t); \
+  template size_t workspace_typed<T>(pp_scan_algo, const void*, const void*, uint64_t);
+
+}  // namespace capi
+}  // namespace pp

@@ -1,0 +1,385 @@
+// Host-side launch layer shared by the C ABI (libppgb300.so) and the
+// header-only C++ API (include/parallel_primitives/*.hpp):
+//   * per-(device, stream) cached workspaces, grown stream-ordered with
+//     cudaMallocAsync and zero-filled once (the epoch protocol then keeps
+//     them valid across calls and graph replays without another fill);
+//   * occupancy-based persistent grid sizing (replaces get_max_occupancy,
+//     include/cooperative_groups.hpp:150-167);
+//   * the launch functions for every kernel template.
+// Nothing here synchronises the stream except the explicit *_sync helpers.
+#pragma once
+
+#include <atomic>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <utility>
+
+#include <cuda_runtime.h>
+
+#include "cooperative_scan.cuh"
+#include "decoupled_scan.cuh"
+#include "reduce.cuh"
+#include "scan_policy.cuh"
+#include "workspace.cuh"
+
+namespace pp {
+namespace host {
+
+enum class Status : int {
+  ok = 0,
+  invalid_arg = 1,
+  unsupported = 2,
+  grid_too_large = 3,
+  timeout = 4,
+  cuda = 5,
+  workspace = 6,
+  no_device = 7,
+};
+
+struct Settings {
+  std::atomic<unsigned long long> timeout_ns{1000000000ull};  // every device wait gives up after 1 s
+  std::atomic<long long> debug_skip_tile{-1};
+  std::atomic<int> max_ctas{0};  // 0 = occupancy x SMs
+};
+inline Settings& settings() {
+  static Settings s;
+  return s;
+}
+
+inline Status from_cuda(cudaError_t e) { return e == cudaSuccess ? Status::ok : Status::cuda; }
+
+struct DeviceInfo {
+  int sm_count = 0;
+  int smem_optin = 0;
+  bool valid = false;
+};
+
+inline Status device_info(DeviceInfo& out) {
+  static std::mutex mu;
+  static std::map<int, DeviceInfo> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return Status::no_device;
+  std::lock_guard<std::mutex> g(mu);
+  DeviceInfo& d = cache[dev];
+  if (!d.valid) {
+    if (cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return Status::no_device;
+    cudaDeviceGetAttribute(&d.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    d.valid = true;
+  }
+  out = d;
+  return Status::ok;
+}
+
+// ---------------------------------------------------------------------------
+// Workspace cache: one zero-initialised buffer per (device, stream). Calls on
+// the same stream are ordered, so they may share it; calls on different
+// streams never do.
+class WorkspaceCache {
+ public:
+  Status get(cudaStream_t s, size_t need, void** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return Status::no_device;
+    std::lock_guard<std::mutex> g(mu_);
+    Entry& e = map_[{dev, reinterpret_cast<uintptr_t>(s)}];
+    if (e.bytes >= need) {
+      *out = e.ptr;
+      return Status::ok;
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) return Status::cuda;
+    if (cs != cudaStreamCaptureStatusNone) return Status::workspace;  // size it before capturing
+    size_t nb = need;
+    if (nb < (size_t(1) << 20)) nb = size_t(1) << 20;
+    if (nb < e.bytes * 2) nb = e.bytes * 2;
+    nb = (nb + 4095) & ~size_t(4095);
+    void* p = nullptr;
+    if (cudaMallocAsync(&p, nb, s) != cudaSuccess) return Status::cuda;
+    if (cudaMemsetAsync(p, 0, nb, s) != cudaSuccess) return Status::cuda;
+    if (e.ptr) cudaFreeAsync(e.ptr, s);
+    e.ptr = p;
+    e.bytes = nb;
+    *out = p;
+    return Status::ok;
+  }
+  // Returns the workspace of this stream if one exists.
+  void* find(cudaStream_t s) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> g(mu_);
+    auto it = map_.find({dev, reinterpret_cast<uintptr_t>(s)});
+    return it == map_.end() ? nullptr : it->second.ptr;
+  }
+  static WorkspaceCache& instance() {
+    static WorkspaceCache* c = new WorkspaceCache();  // never destroyed: outlives CUDA teardown
+    return *c;
+  }
+
+ private:
+  struct Entry {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+  };
+  std::mutex mu_;
+  std::map<std::pair<int, uintptr_t>, Entry> map_;
+};
+
+// A workspace either supplied by the caller (must have been zero-filled once
+// before its first use, and must not be shared by calls that overlap on the
+// GPU) or taken from the per-stream cache.
+struct Ws {
+  WsHeader* hdr = nullptr;
+  void* aux = nullptr;
+  uint64_t* desc = nullptr;
+};
+
+inline Status acquire_ws(cudaStream_t s, size_t need, void* user_ws, size_t user_bytes, Ws& w) {
+  void* p = user_ws;
+  if (p) {
+    if (user_bytes < need) return Status::workspace;
+    if (reinterpret_cast<uintptr_t>(p) & 255u) return Status::invalid_arg;
+  } else {
+    Status st = WorkspaceCache::instance().get(s, need, &p);
+    if (st != Status::ok) return st;
+  }
+  w.hdr = static_cast<WsHeader*>(p);
+  w.aux = static_cast<unsigned char*>(p) + kHeaderBytes;
+  w.desc = reinterpret_cast<uint64_t*>(static_cast<unsigned char*>(p) + kDescOffset);
+  return Status::ok;
+}
+
+// Copies the sticky device error word of a workspace to the host, clears it
+// and returns it as a Status. Synchronises `s`.
+inline Status read_device_error(cudaStream_t s, void* ws) {
+  if (!ws) {
+    ws = WorkspaceCache::instance().find(s);
+    if (!ws) return from_cuda(cudaStreamSynchronize(s));
+  }
+  WsHeader* h = static_cast<WsHeader*>(ws);
+  unsigned int err = 0;
+  cudaError_t e = cudaMemcpyAsync(&err, &h->error, sizeof(err), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return Status::cuda;
+  if (err != 0) {
+    const unsigned int zero = 0;
+    cudaMemcpyAsync(&h->error, &zero, sizeof(zero), cudaMemcpyHostToDevice, s);
+    cudaStreamSynchronize(s);
+    return static_cast<Status>(err);
+  }
+  return Status::ok;
+}
+
+template <class K>
+inline Status prepare_kernel(K kernel, int threads, size_t smem, int& blocks_per_sm) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, int> cache;  // (kernel, device) -> blocks/SM
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return Status::no_device;
+  std::lock_guard<std::mutex> g(mu);
+  auto key = std::make_pair(reinterpret_cast<const void*>(kernel), dev);
+  auto it = cache.find(key);
+  if (it != cache.end()) {
+    blocks_per_sm = it->second;
+    return Status::ok;
+  }
+  if (smem > 48 * 1024) {
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
+      return Status::cuda;
+  }
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, threads, smem) != cudaSuccess) return Status::cuda;
+  if (b < 1) return Status::unsupported;
+  cache[key] = b;
+  blocks_per_sm = b;
+  return Status::ok;
+}
+
+// ---------------------------------------------------------------------------
+// Decoupled look-back scan.
+template <class Pol>
+struct DecoupledTuning {
+  static constexpr int NC = 8;      // consumer warps
+  static constexpr int CH = 4;      // 16-byte chunks per thread per tile
+  static constexpr int STAGES = 3;  // shared-memory ring depth
+  static constexpr int GEN_NC = 8;
+  static constexpr int GEN_IPT = 8;
+};
+
+template <class Pol>
+inline bool tma_path_ok(const void* in, const void* out) {
+  using in_t = typename Pol::in_t;
+  if constexpr (16 % sizeof(in_t) != 0 || sizeof(typename Pol::out_t) != sizeof(in_t)) {
+    return false;
+  } else {
+    return ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u) == 0;
+  }
+}
+
+template <class Pol>
+inline uint64_t decoupled_tile_elems(const void* in, const void* out) {
+  using Tn = DecoupledTuning<Pol>;
+  if constexpr (16 % sizeof(typename Pol::in_t) == 0) {
+    if (tma_path_ok<Pol>(in, out)) return DecoupledTmaCfg<Pol, Tn::NC, Tn::CH, Tn::STAGES>::TILE;
+  }
+  return DecoupledGenericCfg<Pol, Tn::GEN_NC, Tn::GEN_IPT>::TILE;
+}
+
+template <class Pol>
+inline size_t decoupled_workspace_bytes(uint64_t n, const void* in, const void* out) {
+  const uint64_t tile = decoupled_tile_elems<Pol>(in, out);
+  const uint64_t ntiles = (n + tile - 1) / tile;
+  return workspace_bytes_for_desc_words(ntiles * desc_codec<typename Pol::carry_t>::W);
+}
+
+// grid_ctas: 0 = persistent grid (occupancy x SMs); otherwise the CTA count
+// (1 gives the single work-group scan of scan.hpp:125-130).
+template <class Pol>
+inline Status decoupled_scan(cudaStream_t s, const void* in, void* out, uint64_t n, bool exclusive,
+                             void* user_ws = nullptr, size_t user_ws_bytes = 0, int grid_ctas = 0) {
+  if (n == 0) return Status::ok;
+  if (!in || !out) return Status::invalid_arg;
+  using Tn = DecoupledTuning<Pol>;
+  DeviceInfo di;
+  Status st = device_info(di);
+  if (st != Status::ok) return st;
+  Ws w;
+  st = acquire_ws(s, decoupled_workspace_bytes<Pol>(n, in, out), user_ws, user_ws_bytes, w);
+  if (st != Status::ok) return st;
+  ScanArgs a{};
+  a.in = in;
+  a.out = out;
+  a.n = n;
+  a.hdr = w.hdr;
+  a.desc = w.desc;
+  a.timeout_ns = settings().timeout_ns.load();
+  a.debug_skip_tile = settings().debug_skip_tile.load();
+  a.exclusive = exclusive ? 1 : 0;
+  const int cap = grid_ctas > 0 ? grid_ctas : settings().max_ctas.load();
+  if constexpr (16 % sizeof(typename Pol::in_t) == 0) {
+    if (tma_path_ok<Pol>(in, out)) {
+      using Cfg = DecoupledTmaCfg<Pol, Tn::NC, Tn::CH, Tn::STAGES>;
+      auto k = decoupled_tma_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES>;
+      int bps = 0;
+      st = prepare_kernel(k, Cfg::THREADS, Cfg::SMEM, bps);
+      if (st != Status::ok) return st;
+      const uint64_t ntiles = (n + Cfg::TILE - 1) / Cfg::TILE;
+      uint64_t grid = uint64_t(bps) * di.sm_count;
+      if (cap > 0 && uint64_t(cap) < grid) grid = cap;
+      if (ntiles < grid) grid = ntiles;
+      k<<<unsigned(grid), Cfg::THREADS, Cfg::SMEM, s>>>(a);
+      return from_cuda(cudaGetLastError());
+    }
+  }
+  using Cfg = DecoupledGenericCfg<Pol, Tn::GEN_NC, Tn::GEN_IPT>;
+  auto k = decoupled_generic_kernel<Pol, Tn::GEN_NC, Tn::GEN_IPT>;
+  int bps = 0;
+  st = prepare_kernel(k, Cfg::THREADS, 0, bps);
+  if (st != Status::ok) return st;
+  const uint64_t ntiles = (n + Cfg::TILE - 1) / Cfg::TILE;
+  uint64_t grid = uint64_t(bps) * di.sm_count;
+  if (cap > 0 && uint64_t(cap) < grid) grid = cap;
+  if (ntiles < grid) grid = ntiles;
+  k<<<unsigned(grid), Cfg::THREADS, 0, s>>>(a);
+  return from_cuda(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
+// Cooperative grid-barrier scan.
+template <class Pol>
+struct CoopTuning {
+  static constexpr int NC = 8;
+  static constexpr int CH = 4;
+};
+
+// grid_ctas: 0 = every block the device holds co-resident; a larger request
+// than that fails with grid_too_large (the reference's perform_check,
+// include/cooperative_groups.hpp:65-76).
+template <class Pol>
+inline Status cooperative_scan(cudaStream_t s, const void* in, void* out, uint64_t n, bool exclusive,
+                               void* user_ws = nullptr, size_t user_ws_bytes = 0, int grid_ctas = 0) {
+  if (n == 0) return Status::ok;
+  if (!in || !out) return Status::invalid_arg;
+  using Tn = CoopTuning<Pol>;
+  using Cfg = CoopCfg<Pol, Tn::NC, Tn::CH>;
+  DeviceInfo di;
+  Status st = device_info(di);
+  if (st != Status::ok) return st;
+  auto k = cooperative_scan_kernel<Pol, Tn::NC, Tn::CH>;
+  int bps = 0;
+  st = prepare_kernel(k, Cfg::THREADS, 0, bps);
+  if (st != Status::ok) return st;
+  const uint64_t max_grid = uint64_t(bps) * di.sm_count;
+  uint64_t grid = max_grid;
+  if (grid_ctas > 0) {
+    if (uint64_t(grid_ctas) > max_grid) return Status::grid_too_large;
+    grid = grid_ctas;
+  } else if (settings().max_ctas.load() > 0 && uint64_t(settings().max_ctas.load()) < grid) {
+    grid = settings().max_ctas.load();
+  }
+  const uint64_t ntiles = (n + Cfg::TILE - 1) / Cfg::TILE;
+  if (ntiles < grid) grid = ntiles;
+  if (grid > uint64_t(kMaxPartials)) grid = kMaxPartials;
+  Ws w;
+  st = acquire_ws(s, workspace_bytes_for_desc_words(0), user_ws, user_ws_bytes, w);
+  if (st != Status::ok) return st;
+  CoopArgs ca{};
+  ca.s.in = in;
+  ca.s.out = out;
+  ca.s.n = n;
+  ca.s.hdr = w.hdr;
+  ca.s.desc = w.desc;
+  ca.s.timeout_ns = settings().timeout_ns.load();
+  ca.s.debug_skip_tile = -1;
+  ca.s.exclusive = exclusive ? 1 : 0;
+  ca.block_aggs = w.aux;
+  void* params[] = {&ca};
+  return from_cuda(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k), dim3(unsigned(grid)),
+                                               dim3(Cfg::THREADS), params, 0, s));
+}
+
+// ---------------------------------------------------------------------------
+// Reduction: result written to device memory (d_result, one T).
+template <class T, class Op>
+struct ReduceTuning {
+  static constexpr int BLOCK = 512;
+  static constexpr int UNROLL = 4;
+};
+
+template <class T, class Op>
+inline Status reduce(cudaStream_t s, const T* in, uint64_t n, T* d_result, void* user_ws = nullptr,
+                     size_t user_ws_bytes = 0) {
+  if (!d_result || (n > 0 && !in)) return Status::invalid_arg;
+  using Tn = ReduceTuning<T, Op>;
+  DeviceInfo di;
+  Status st = device_info(di);
+  if (st != Status::ok) return st;
+  auto k = reduce_kernel<T, Op, Tn::BLOCK, Tn::UNROLL>;
+  int bps = 0;
+  st = prepare_kernel(k, Tn::BLOCK, 0, bps);
+  if (st != Status::ok) return st;
+  Ws w;
+  st = acquire_ws(s, workspace_bytes_for_desc_words(0), user_ws, user_ws_bytes, w);
+  if (st != Status::ok) return st;
+  constexpr int V = (16 % sizeof(T) == 0) ? int(16 / sizeof(T)) : 1;
+  uint64_t grid = uint64_t(bps) * di.sm_count;
+  const int cap = settings().max_ctas.load();
+  if (cap > 0 && uint64_t(cap) < grid) grid = cap;
+  // no more blocks than there are vectors to hand out
+  const uint64_t work_blocks = (n / V + Tn::BLOCK - 1) / Tn::BLOCK;
+  if (work_blocks < grid) grid = work_blocks;
+  if (grid < 1) grid = 1;
+  if (grid > uint64_t(kMaxPartials)) grid = kMaxPartials;
+  ReduceArgs a{};
+  a.in = in;
+  a.n = n;
+  a.result = d_result;
+  a.hdr = w.hdr;
+  a.partials = w.aux;
+  k<<<unsigned(grid), Tn::BLOCK, 0, s>>>(a);
+  return from_cuda(cudaGetLastError());
+}
+
+}  // namespace host
+}  // namespace pp

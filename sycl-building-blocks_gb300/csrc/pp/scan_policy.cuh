@@ -1,0 +1,125 @@
+// Scan policies: how an input element becomes an in-tile accumulator, how
+// the cross-tile carry (look-back descriptor payload) is represented, and how
+// an output element is formed from the carry and the in-tile prefix.
+//
+//   acc_t    in-tile accumulator (thread / warp / block scans)
+//   carry_t  tile aggregate and look-back carry (descriptor payload)
+//   pre_t    per-thread prepared carry used to finish outputs
+//
+// PlainScan is the reference's semantics (one type, one operator).
+// CompensatedF32 keeps float-float (hi, lo) pairs everywhere: TwoSum
+// accumulation for the tile aggregates, the carries and the in-tile prefixes.
+// F64CarryF32 keeps the in-tile work in FP32 and only the cross-tile carry
+// chain in FP64.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ops.cuh"
+
+namespace pp {
+
+template <class T, class Op>
+struct PlainScan {
+  using in_t = T;
+  using out_t = T;
+  using acc_t = T;
+  using carry_t = T;
+  using pre_t = T;
+  Op op;
+
+  __device__ __forceinline__ acc_t load(const in_t& x) const { return x; }
+  __device__ __forceinline__ acc_t aop(const acc_t& a, const acc_t& b) const { return op(a, b); }
+  __device__ __forceinline__ acc_t aid() const { return identity<Op, T>(); }
+  __device__ __forceinline__ carry_t to_carry(const acc_t& a) const { return a; }
+  __device__ __forceinline__ carry_t cop(const carry_t& a, const carry_t& b) const { return op(a, b); }
+  __device__ __forceinline__ carry_t cid() const { return identity<Op, T>(); }
+  __device__ __forceinline__ pre_t prepare(const carry_t& c) const { return c; }
+  __device__ __forceinline__ pre_t extend(const pre_t& p, const acc_t& a) const { return op(p, a); }
+  __device__ __forceinline__ out_t finish(const pre_t& p, const acc_t& a) const { return op(p, a); }
+  __device__ __forceinline__ out_t finish_first(const pre_t& p) const { return p; }
+};
+
+// float-float pair: value = hi + lo, |lo| <= ulp(hi)/2.
+struct ff32 {
+  float hi, lo;
+};
+
+// Knuth TwoSum: s + e == a + b exactly (round-to-nearest, no FMA involved).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// Dekker FastTwoSum, exact when |a| >= |b| (or a == 0).
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+// Pair + pair ("sloppy" double-word addition): absolute error O(u^2 (|x|+|y|)).
+__device__ __forceinline__ ff32 ff_add(const ff32& x, const ff32& y) {
+  float s, e;
+  two_sum(x.hi, y.hi, s, e);
+  e = __fadd_rn(e, __fadd_rn(x.lo, y.lo));
+  ff32 r;
+  fast_two_sum(s, e, r.hi, r.lo);
+  return r;
+}
+// Pair + float.
+__device__ __forceinline__ ff32 ff_add_f(const ff32& x, float y) {
+  float s, e;
+  two_sum(x.hi, y, s, e);
+  e = __fadd_rn(e, x.lo);
+  ff32 r;
+  fast_two_sum(s, e, r.hi, r.lo);
+  return r;
+}
+
+struct CompensatedF32 {
+  using in_t = float;
+  using out_t = float;
+  using acc_t = ff32;
+  using carry_t = ff32;
+  using pre_t = ff32;
+
+  __device__ __forceinline__ acc_t load(const float& x) const { return ff32{x, 0.0f}; }
+  __device__ __forceinline__ acc_t aop(const acc_t& a, const acc_t& b) const { return ff_add(a, b); }
+  __device__ __forceinline__ acc_t aid() const { return ff32{0.0f, 0.0f}; }
+  __device__ __forceinline__ carry_t to_carry(const acc_t& a) const { return a; }
+  __device__ __forceinline__ carry_t cop(const carry_t& a, const carry_t& b) const { return ff_add(a, b); }
+  __device__ __forceinline__ carry_t cid() const { return ff32{0.0f, 0.0f}; }
+  __device__ __forceinline__ pre_t prepare(const carry_t& c) const { return c; }
+  __device__ __forceinline__ pre_t extend(const pre_t& p, const acc_t& a) const { return ff_add(p, a); }
+  __device__ __forceinline__ out_t finish(const pre_t& p, const acc_t& a) const {
+    float s, e;
+    two_sum(p.hi, a.hi, s, e);
+    return __fadd_rn(s, __fadd_rn(e, __fadd_rn(p.lo, a.lo)));
+  }
+  __device__ __forceinline__ out_t finish_first(const pre_t& p) const { return __fadd_rn(p.hi, p.lo); }
+};
+
+struct F64CarryF32 {
+  using in_t = float;
+  using out_t = float;
+  using acc_t = float;
+  using carry_t = double;
+  using pre_t = ff32;
+
+  __device__ __forceinline__ acc_t load(const float& x) const { return x; }
+  __device__ __forceinline__ acc_t aop(const acc_t& a, const acc_t& b) const { return __fadd_rn(a, b); }
+  __device__ __forceinline__ acc_t aid() const { return 0.0f; }
+  __device__ __forceinline__ carry_t to_carry(const acc_t& a) const { return double(a); }
+  __device__ __forceinline__ carry_t cop(const carry_t& a, const carry_t& b) const { return __dadd_rn(a, b); }
+  __device__ __forceinline__ carry_t cid() const { return 0.0; }
+  __device__ __forceinline__ pre_t prepare(const carry_t& c) const {
+    const float hi = __double2float_rn(c);
+    return ff32{hi, __double2float_rn(__dsub_rn(c, double(hi)))};
+  }
+  __device__ __forceinline__ pre_t extend(const pre_t& p, const acc_t& a) const { return ff_add_f(p, a); }
+  __device__ __forceinline__ out_t finish(const pre_t& p, const acc_t& a) const {
+    return __fadd_rn(p.hi, __fadd_rn(p.lo, a));
+  }
+  __device__ __forceinline__ out_t finish_first(const pre_t& p) const { return __fadd_rn(p.hi, p.lo); }
+};
+
+}  // namespace pp

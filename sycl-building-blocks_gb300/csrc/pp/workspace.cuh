@@ -1,0 +1,168 @@
+// Device workspace shared by the scan / reduce kernels, and the packed
+// look-back descriptors.
+//
+// Layout (one contiguous, 256-byte aligned device buffer):
+//   [0, 4096)                      WsHeader: ticket counter, CTA exit counter,
+//                                  epoch, sticky error word, abort flag, grid
+//                                  barrier words.
+//   [4096, 4096 + kAuxBytes)       per-block partials (reduction, cooperative
+//                                  scan block aggregates).
+//   [4096 + kAuxBytes, ...)        look-back descriptors, desc_words() 64-bit
+//                                  words per tile.
+//
+// Descriptor words replace the reference's unpacked partition_descriptor
+// {inclusive_prefix_, aggregate_, status} (include/parallel_primitives/
+// internal/partition_descriptor.h:92-141, status enum :10-14). Each 64-bit
+// word is {tag:32 | payload:32} with tag = (epoch << 2) | status, status
+// 1 = aggregate available, 2 = inclusive prefix available, anything else
+// invalid. A value wider than 32 bits is split over 2 or 4 words that all
+// carry the tag; a reader accepts a descriptor only when every word carries
+// the same current-epoch tag, so a half-updated descriptor reads as invalid.
+// Every word is written with one st.relaxed.gpu and read with ld.relaxed.gpu:
+// the payload travels with its flag, so no fence is needed on either side.
+//
+// The epoch removes the per-call descriptor fill of the reference
+// (scan_decoupled_lookback.hpp:115-116): the last CTA of every launch bumps
+// the epoch and re-arms the ticket and exit counters, so back-to-back calls
+// and CUDA-graph replays need no memset node. When the 30-bit epoch wraps the
+// last CTA clears every descriptor word ever used (high-water mark).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "ptx.cuh"
+#include "warp.cuh"
+
+namespace pp {
+
+// Status codes shared with the C ABI (include/pp_gb300.h).
+enum DeviceError : uint32_t {
+  kDevOk = 0,
+  kDevTimeout = 4,
+};
+
+struct WsHeader {
+  unsigned long long ticket;          // next tile ticket
+  unsigned long long desc_words_hwm;  // descriptor words ever used
+  unsigned long long error_detail;    // e.g. the tile whose wait gave up
+  unsigned int done;                  // CTAs that have exited this launch
+  unsigned int epoch;                 // in [0, kEpochLimit): tags use epoch + 1
+  unsigned int error;                 // first device error, sticky until read
+  unsigned int abort;                 // set on a timeout; every spin exits
+  unsigned int bar_count;             // grid barrier arrivals
+  unsigned int bar_gen;               // grid barrier generation
+  unsigned int debug_spin;            // unused padding / diagnostics
+  unsigned int pad_;
+};
+
+constexpr size_t kHeaderBytes = 4096;
+constexpr int kMaxPartials = 8192;                 // blocks with a partial slot
+constexpr size_t kAuxBytes = size_t(kMaxPartials) * 16;
+constexpr size_t kDescOffset = kHeaderBytes + kAuxBytes;
+constexpr uint32_t kEpochLimit = (1u << 30) - 1;  // tag epoch = epoch + 1 in [1, 2^30)
+
+enum DescStatus : uint32_t { kInvalid = 0, kAggregate = 1, kPrefix = 2 };
+
+__host__ __device__ constexpr size_t workspace_bytes_for_desc_words(uint64_t words) {
+  return kDescOffset + words * 8;
+}
+
+template <class C>
+struct desc_codec {
+  static constexpr int PW = (sizeof(C) + 3) / 4;  // 32-bit payload words
+  static_assert(PW <= 4, "look-back carries wider than 16 bytes are not supported");
+  static constexpr int W = PW == 1 ? 1 : (PW == 2 ? 2 : 4);  // 64-bit descriptor words
+
+  __device__ __forceinline__ static void publish(uint64_t* d, const C& v, uint32_t tag) {
+    words<C> p = to_words(v);
+    const uint64_t hi = uint64_t(tag) << 32;
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      const uint32_t w = i < PW ? p.w[i < PW ? i : 0] : 0u;
+      ptx::st_relaxed(d + i, hi | w);
+    }
+  }
+
+  // Returns the status of descriptor `d` in epoch tag `etag` (= epoch+1) and
+  // its payload in `v`; kInvalid when not (fully) written in this epoch.
+  __device__ __forceinline__ static uint32_t read(const uint64_t* d, uint32_t etag, C& v) {
+    uint64_t w[W];
+    if constexpr (W == 1) {
+      w[0] = ptx::ld_relaxed(d);
+    } else {
+#pragma unroll
+      for (int i = 0; i < W; i += 2) ptx::ld_relaxed_v2(d + i, w[i], w[i + 1]);
+    }
+    const uint32_t tag = uint32_t(w[0] >> 32);
+    bool same = true;
+#pragma unroll
+    for (int i = 1; i < W; ++i) same &= uint32_t(w[i] >> 32) == tag;
+    const uint32_t st = tag & 3u;
+    if (!same || (tag >> 2) != etag || (st != kAggregate && st != kPrefix)) return kInvalid;
+    words<C> p;
+#pragma unroll
+    for (int i = 0; i < PW; ++i) p.w[i] = uint32_t(w[i]);
+    v = from_words<C>(p);
+    return st;
+  }
+};
+
+__device__ __forceinline__ uint32_t make_tag(uint32_t etag, uint32_t status) {
+  return (etag << 2) | status;
+}
+
+// Records the first device error and raises the abort flag.
+__device__ __forceinline__ void raise_error(WsHeader* h, uint32_t code, unsigned long long detail) {
+  if (atomicCAS(&h->error, 0u, code) == 0u) h->error_detail = detail;
+  atomicExch(&h->abort, 1u);
+}
+
+__device__ __forceinline__ bool aborted(WsHeader* h) {
+  return ptx::ld_relaxed(reinterpret_cast<const uint32_t*>(&h->abort)) != 0u;
+}
+
+// Bounded wait on an mbarrier phase. Returns false (after raising a timeout)
+// when the phase has not completed within timeout_ns or another CTA aborted.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, WsHeader* h,
+                                                  uint64_t timeout_ns, unsigned long long detail) {
+  if (ptx::mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = ptx::globaltimer_ns();
+  for (uint32_t it = 1;; ++it) {
+    if (ptx::mbar_try_wait(bar, parity)) return true;
+    if ((it & 15u) == 0u) {
+      if (aborted(h)) return false;
+      if (ptx::globaltimer_ns() - t0 > timeout_ns) {
+        raise_error(h, kDevTimeout, detail);
+        return false;
+      }
+    }
+  }
+}
+
+// Called by thread 0 of every CTA after the CTA's last access to the shared
+// control words. The last CTA to exit re-arms the workspace for the next
+// launch on the same stream: ticket and exit counters to zero, abort cleared,
+// epoch advanced (clearing all descriptors when the epoch wraps).
+__device__ __forceinline__ void cta_exit_rearm(WsHeader* h, uint64_t* desc, uint64_t desc_words_used) {
+  __threadfence();
+  const unsigned prev = atomicAdd(&h->done, 1u);
+  if (prev != gridDim.x - 1) return;
+  __threadfence();
+  unsigned long long hwm = h->desc_words_hwm;
+  if (desc_words_used > hwm) hwm = desc_words_used;
+  h->desc_words_hwm = hwm;
+  uint32_t next = h->epoch + 1;
+  if (next >= kEpochLimit) {
+    for (unsigned long long i = 0; i < hwm; ++i) desc[i] = 0ull;
+    next = 0;
+  }
+  h->epoch = next;
+  h->ticket = 0ull;
+  h->abort = 0u;
+  h->bar_count = 0u;
+  __threadfence();
+  h->done = 0u;
+}
+
+}  // namespace pp

@@ -1,0 +1,183 @@
+"""GPU parity of the decoupled look-back scan (and its single-group and
+cooperative variants) against the CPU oracle, through the C ABI.
+
+Integer results are compared bit for bit; float plus-scans against the FP64
+oracle within the bound in helpers.float_scan_bound; min/max bit for bit."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import (FLOAT_DTYPES, FLOAT_OPS, INT_DTYPES, INT_OPS, NP, check_scan, empty_dev, from_dev,
+                     make_input, to_dev)
+
+pytestmark = pytest.mark.gpu
+
+# sizes around the tile edges of both kernels (TMA tile: 4096 x 4-byte or
+# 2048 x 8-byte elements; generic tile: 2048 elements), ragged tails and
+# lengths whose byte count is not a multiple of 16
+SIZES = [1, 2, 3, 31, 32, 33, 2047, 2048, 2049, 4095, 4096, 4097, 12289, 65537, 1000003]
+ALL = [(d, o) for d in INT_DTYPES for o in INT_OPS] + [(d, o) for d in FLOAT_DTYPES for o in FLOAT_OPS]
+
+
+def _tiles(n):
+    return (n + 1023) // 1024
+
+
+def _run(pp, cuda, x, dtype, op, excl, algo="auto", offset=0, inplace=False):
+    n = x.size
+    d_in = to_dev(cuda, np.concatenate([np.zeros(offset, dtype=x.dtype), x]))
+    if inplace:
+        d_out = d_in
+    else:
+        d_out = empty_dev(cuda, n, NP[dtype], pad=offset)
+    esz = x.dtype.itemsize
+    stream = cuda.cuda.current_stream().cuda_stream
+    pp.scan("exclusive" if excl else "inclusive", op, d_in.data_ptr() + offset * esz,
+            d_out.data_ptr() + offset * esz, n, dtype, stream=stream, algo=algo)
+    assert pp.stream_status(stream) == 0
+    return from_dev(d_out, NP[dtype])[offset:]
+
+
+@pytest.mark.parametrize("dtype,op", ALL)
+@pytest.mark.parametrize("excl", [False, True])
+def test_decoupled_all_ops(pp, oracle, cuda, dtype, op, excl):
+    for i, n in enumerate([1, 33, 4097, 65537, 300007]):
+        x = make_input(dtype, op, n, seed=1000 + 17 * i + len(op))
+        got = _run(pp, cuda, x, dtype, op, excl)
+        check_scan(got, x, dtype, op, excl, _tiles(n))
+
+
+@pytest.mark.parametrize("n", SIZES)
+@pytest.mark.parametrize("dtype", ["u32", "u64", "f32"])
+def test_decoupled_sizes(pp, oracle, cuda, n, dtype):
+    x = make_input(dtype, "plus", n, seed=n)
+    for excl in (False, True):
+        check_scan(_run(pp, cuda, x, dtype, "plus", excl), x, dtype, "plus", excl, _tiles(n))
+
+
+@pytest.mark.parametrize("dtype", ["u32", "i64", "f64"])
+@pytest.mark.parametrize("offset", [1, 3])
+def test_unaligned_pointers_take_generic_path(pp, oracle, cuda, dtype, offset):
+    n = 70001
+    x = make_input(dtype, "plus", n, seed=5 + offset)
+    for excl in (False, True):
+        check_scan(_run(pp, cuda, x, dtype, "plus", excl, offset=offset), x, dtype, "plus", excl, _tiles(n))
+
+
+@pytest.mark.parametrize("dtype", ["u32", "u64"])
+def test_in_place(pp, oracle, cuda, dtype):
+    n = 1 << 20
+    x = make_input(dtype, "plus", n, seed=99)
+    for excl in (False, True):
+        check_scan(_run(pp, cuda, x, dtype, "plus", excl, inplace=True), x, dtype, "plus", excl, _tiles(n))
+
+
+@pytest.mark.parametrize("algo", ["single_group", "cooperative"])
+@pytest.mark.parametrize("dtype,op", [("u32", "plus"), ("i32", "maximum"), ("u64", "plus"), ("i64", "bit_xor"),
+                                      ("f32", "plus"), ("f64", "minimum")])
+def test_other_algorithms(pp, oracle, cuda, algo, dtype, op):
+    for n in (1, 4095, 4097, 200003):
+        x = make_input(dtype, op, n, seed=3 * n + 1)
+        for excl in (False, True):
+            check_scan(_run(pp, cuda, x, dtype, op, excl, algo=algo), x, dtype, op, excl, _tiles(n))
+
+
+def test_cooperative_unaligned(pp, oracle, cuda):
+    n = 123457
+    x = make_input("u32", "plus", n, seed=4)
+    check_scan(_run(pp, cuda, x, "u32", "plus", False, algo="cooperative", offset=1), x, "u32", "plus", False,
+               _tiles(n))
+
+
+def test_reference_benchmark_known_answer(pp, cuda):
+    """benchmarks/benchmark_scan.cpp:32-51: fill(1) -> out[n-1] == n."""
+    n = (1 << 24) + 5
+    d = cuda.ones(n, dtype=cuda.int32, device="cuda")
+    o = cuda.empty_like(d)
+    s = cuda.cuda.current_stream().cuda_stream
+    pp.decoupled_scan_device("inclusive", "plus", d.data_ptr(), o.data_ptr(), n, "u32", stream=s)
+    assert int(o[-1]) == n
+    assert cuda.equal(o[:1000].cpu(), cuda.arange(1, 1001, dtype=cuda.int32))
+
+
+def test_many_calls_and_streams(pp, oracle, cuda):
+    """Back-to-back calls re-use the per-stream workspace (epoch protocol);
+    two streams get two workspaces."""
+    xs = [make_input("u32", "plus", n, seed=n) for n in (5000, 300000, 17, 1 << 18)]
+    want = [oracle.scan(x, "plus") for x in xs]
+    streams = [cuda.cuda.Stream(), cuda.cuda.Stream()]
+    dev_in = [to_dev(cuda, x) for x in xs]
+    dev_out = [cuda.empty_like(d) for d in dev_in]
+    cuda.cuda.synchronize()
+    for rep in range(25):
+        for k, (di, do) in enumerate(zip(dev_in, dev_out)):
+            s = streams[(rep + k) % 2]
+            with cuda.cuda.stream(s):
+                do.zero_()
+                pp.decoupled_scan_device("inclusive", "plus", di.data_ptr(), do.data_ptr(), di.numel(), "u32",
+                                         stream=s.cuda_stream)
+        cuda.cuda.synchronize()
+        for k, do in enumerate(dev_out):
+            assert np.array_equal(from_dev(do, np.uint32), want[k]), (rep, k)
+    for s in streams:
+        assert pp.stream_status(s.cuda_stream) == 0
+
+
+def test_caller_workspace(pp, oracle, cuda):
+    n = 777777
+    x = make_input("u64", "plus", n, seed=12)
+    d_in = to_dev(cuda, x)
+    d_out = cuda.empty_like(d_in)
+    nbytes = pp.workspace_size("decoupled", "u64", d_in.data_ptr(), d_out.data_ptr(), n)
+    ws = cuda.zeros(nbytes, dtype=cuda.uint8, device="cuda")
+    s = cuda.cuda.current_stream().cuda_stream
+    for _ in range(3):
+        pp.scan("inclusive", "plus", d_in.data_ptr(), d_out.data_ptr(), n, "u64", stream=s,
+                workspace=(ws.data_ptr(), nbytes))
+    assert pp.workspace_status(s, ws.data_ptr()) == 0
+    assert np.array_equal(from_dev(d_out, np.uint64), oracle.scan(x, "plus"))
+    with pytest.raises(pp.PPError) as e:
+        pp.scan("inclusive", "plus", d_in.data_ptr(), d_out.data_ptr(), n, "u64", stream=s,
+                workspace=(ws.data_ptr(), 4096))
+    assert e.value.status == pp.PP_ERR_WORKSPACE
+
+
+def test_lookback_timeout_is_reported_not_hung(pp, oracle, cuda):
+    """A tile that never publishes its descriptor makes its successors' bounded
+    look-back give up: the call returns, the stream reports PP_ERR_TIMEOUT, and
+    the next call on the same stream is correct again."""
+    n = 1 << 20
+    x = make_input("u32", "plus", n, seed=21)
+    d_in = to_dev(cuda, x)
+    d_out = cuda.empty_like(d_in)
+    s = cuda.cuda.current_stream().cuda_stream
+    pp.set_timeout_ns(50_000_000)
+    pp.debug_set_skip_tile(3)
+    try:
+        pp.decoupled_scan_device("inclusive", "plus", d_in.data_ptr(), d_out.data_ptr(), n, "u32", stream=s)
+        assert pp.stream_status(s) == pp.PP_ERR_TIMEOUT
+    finally:
+        pp.debug_set_skip_tile(-1)
+        pp.set_timeout_ns(1_000_000_000)
+    pp.decoupled_scan_device("inclusive", "plus", d_in.data_ptr(), d_out.data_ptr(), n, "u32", stream=s)
+    assert pp.stream_status(s) == 0
+    assert np.array_equal(from_dev(d_out, np.uint32), oracle.scan(x, "plus"))
+
+
+def test_host_wrappers(pp, oracle, cuda):
+    x = make_input("i32", "plus", 300001, seed=8)
+    np.testing.assert_array_equal(pp.decoupled_scan("inclusive", "plus", x), oracle.scan(x, "plus"))
+    np.testing.assert_array_equal(pp.cooperative_scan("exclusive", "plus", x), oracle.scan(x, "plus", True))
+    np.testing.assert_array_equal(pp.scan_host("inclusive", "maximum", x), oracle.scan(x, "maximum"))
+
+
+def test_bad_arguments(pp, cuda):
+    d = cuda.zeros(16, dtype=cuda.float32, device="cuda")
+    with pytest.raises(pp.PPError) as e:
+        pp.scan("inclusive", "bit_and", d.data_ptr(), d.data_ptr(), 16, "f32")
+    assert e.value.status == pp.PP_ERR_UNSUPPORTED
+    with pytest.raises(pp.PPError) as e:
+        pp.scan("inclusive", "plus", d.data_ptr(), d.data_ptr(), 16, "u32", precision="compensated")
+    assert e.value.status == pp.PP_ERR_UNSUPPORTED
