@@ -197,8 +197,8 @@ def run_ours(args) -> dict | None:
     total = int(d_in.to(torch.int64).sum().item()) & 0xFFFFFFFF
     verified = (int(d_out[-1].item()) & 0xFFFFFFFF) == total and int(d_out[0].item()) == int(d_in[0].item())
 
-    gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0] or 0) if \
-        os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else local
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0]
+    gpu_index = int(vis) if vis.isdigit() else local
     sampler = ClockSampler(gpu_index)
     sampler.start()
     time.sleep(0.2)
@@ -244,7 +244,7 @@ def run_ours(args) -> dict | None:
     barrier(torch)
     e2e_s = max_over_ranks(torch, time.perf_counter() - t0)
     e2e_value = ws * algo_bytes * e2e_steps / e2e_s / 1e9
-    e2e_ok = bool(np.array_equal(h_out[-4:].numpy(), d_out[-4:].cpu().numpy()))
+    e2e_ok = (int(h_out[-1]) & 0xFFFFFFFF) == total and int(h_out[0]) == int(h_in[0])
     del h_in, h_out
 
     cpu = None

@@ -50,7 +50,7 @@ def build_ref(force: bool = False) -> Path | None:
         return REF_LIB
     REF_DIR.mkdir(exist_ok=True)
     tmp = REF_LIB.with_suffix(".so.tmp")
-    cmd = ["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-pthread", "-w", "-I", str(shim), "-I",
+    cmd = ["g++", "-std=c++20", "-O2", "-fwrapv", "-fPIC", "-shared", "-pthread", "-w", "-I", str(shim), "-I",
            str(REFERENCE_INCLUDE), str(entry), "-o", str(tmp)]
     subprocess.run(cmd, check=True)
     os.replace(tmp, REF_LIB)

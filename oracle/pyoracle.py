@@ -153,3 +153,57 @@ def fnv1a64(a: np.ndarray) -> int:
 
 def num_threads() -> int:
     return int(lib().oracle_num_threads())
+
+
+# ---- the reference's own code on the CPU (oracle/_ref, built where the
+# reference checkout exists) ---------------------------------------------------
+_ref = None
+
+
+def ref_lib():
+    """ctypes handle of oracle/_ref/libsyclref.so, or None when it is absent."""
+    global _ref
+    if _ref is None:
+        from build_oracle import REF_LIB, build_ref  # noqa: local recipe
+
+        path = build_ref() or (REF_LIB if REF_LIB.exists() else None)
+        if path is None:
+            return None
+        try:
+            L = C.CDLL(str(path))
+        except OSError:
+            return None
+        vp, u64, i32 = C.c_void_p, C.c_uint64, C.c_int
+        L.ref_scan.argtypes = [i32, i32, i32, i32, vp, vp, u64]
+        L.ref_reduce.argtypes = [i32, i32, vp, u64, vp]
+        L.ref_funnelshift_l.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32]
+        L.ref_funnelshift_l.restype = C.c_uint32
+        L.ref_funnelshift_r.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32]
+        L.ref_funnelshift_r.restype = C.c_uint32
+        L.ref_brev32.argtypes = [C.c_uint32]
+        L.ref_brev32.restype = C.c_uint32
+        L.ref_brev64.argtypes = [C.c_uint64]
+        L.ref_brev64.restype = C.c_uint64
+        L.ref_upsample.argtypes = [C.c_uint8] * 4
+        L.ref_upsample.restype = C.c_uint32
+        L.ref_num_groups.restype = i32
+        _ref = L
+    return _ref
+
+
+def reference_scan(a: np.ndarray, op="plus", exclusive=False, algo="decoupled") -> np.ndarray:
+    a = np.ascontiguousarray(a)
+    out = np.empty_like(a)
+    rc = ref_lib().ref_scan({"decoupled": 0, "cooperative": 1}[algo], _code(a), _op(op), int(exclusive), _ptr(a),
+                            _ptr(out), a.size)
+    if rc != 0:
+        raise ValueError("unsupported dtype/op")
+    return out
+
+
+def reference_reduce(a: np.ndarray, op="plus"):
+    a = np.ascontiguousarray(a)
+    out = np.zeros(1, dtype=a.dtype)
+    if ref_lib().ref_reduce(_code(a), _op(op), _ptr(a), a.size, _ptr(out)) != 0:
+        raise ValueError("unsupported dtype/op")
+    return out[0]

@@ -6,25 +6,29 @@
 //  * Tiles are handed out by an atomic ticket counter (not by block id), so
 //    every predecessor of a tile belongs to a CTA that is already running:
 //    forward progress holds for any grid size and residency.
-//  * DecoupledTmaKernel: a persistent, warp-specialised kernel. Warp 0 is the
-//    producer: one lane takes tickets and streams whole tiles into a ring of
-//    shared-memory stages with cp.async.bulk (TMA, completion on mbarriers).
-//    The other NC warps consume: 16-byte conflict-free shared loads, a
-//    register scan (thread-serial inside each 16-byte chunk, shuffle
-//    Kogge-Stone across lanes, shared-memory scan across warps), then
-//    coalesced 16-byte streaming stores.
-//  * DecoupledGenericKernel: the same algorithm with plain element loads for
+//  * decoupled_staged_kernel (16-byte aligned data): a persistent,
+//    warp-specialised kernel with one CTA per SM. Warp 0 is the producer: one
+//    lane takes tickets and streams whole 64 KB tiles into a ring of
+//    shared-memory stages with cp.async.bulk (completion on mbarriers). Warp 1
+//    publishes the tile aggregate and runs the look-back. The NC compute warps
+//    reduce tile k+1 out of shared memory while the look-back of tile k is in
+//    flight, then scan tile k (thread-serial inside each 16-byte chunk,
+//    shuffle Kogge-Stone across lanes, warp segments combined through shared
+//    memory) and write it with coalesced 16-byte streaming stores. Large
+//    tiles keep the number of tiles, and so the length of the look-back
+//    chain, small.
+//  * decoupled_generic_kernel: register tiles with plain element loads for
 //    any alignment and any element type (user functors, packed structs).
-//  * Strategy choice of the reference (:143-174): consumer warp 0 peeks at the
-//    predecessor's descriptor when the tile arrives. If the predecessor's
+//  * Strategy choice of the reference (:143-174): the look-back warp peeks at
+//    the predecessor's descriptor when the tile arrives. If the predecessor's
 //    inclusive prefix is already there ("reduce-then-scan"), the tile
 //    publishes its own inclusive prefix straight away and skips the
 //    look-back. Otherwise ("scan-then-reduce") it publishes its aggregate,
 //    runs the look-back and then publishes the prefix.
-//  * The look-back is warp-wide: 32 predecessors per step, the nearest
-//    inclusive prefix found with a ballot, the window folded with an ordered
-//    shuffle reduction (the reference walks one predecessor at a time on one
-//    work-item, partition_descriptor.h:115-130).
+//  * The look-back is warp-wide: LBW windows of 32 predecessors per memory
+//    round trip, the nearest inclusive prefix found with ballots, the windows
+//    folded with ordered shuffle reductions (the reference walks one
+//    predecessor at a time on one work-item, partition_descriptor.h:115-130).
 //  * Every wait is bounded by %globaltimer; a timeout records an error in the
 //    workspace header and makes every CTA leave its loop.
 //  * Combine order is prefix op local everywhere, so associative operators
@@ -33,6 +37,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "scan_policy.cuh"
@@ -52,6 +57,23 @@ struct ScanArgs {
 };
 
 __host__ __device__ constexpr size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Instrumentation hook of the staged kernel: called at fixed points of a
+// tile's life with an event id, the tile index and a value. The default does
+// nothing and compiles away.
+struct NoTrace {
+  __device__ __forceinline__ void operator()(int, long long, unsigned long long) const {}
+};
+enum TraceEvent : int {
+  kTrFull = 0,     // look-back warp sees the tile in shared memory
+  kTrAggPub = 1,   // last compute warp published the tile aggregate
+  kTrAgg = 2,      // look-back warp has the tile aggregate
+  kTrLbDone = 3,   // inclusive prefix published
+  kTrLbRounds = 4, // look-back rounds (value), spins in the upper half
+  kTrSStart = 5,   // compute warp 0 starts the scan pass
+  kTrSDone = 6,    // compute warp 0 finished the scan pass
+  kTrPeek = 7,     // 1 when the predecessor's prefix was there on arrival
+};
 
 // Warp-wide look-back for `tile`. On success writes the combination of the
 // aggregates/prefix of all tiles before `tile` (in sequence order) to `out`.
@@ -185,83 +207,198 @@ struct TileScan {
   }
 };
 
-template <class Pol, int NC_, int CH_, int STAGES_>
-struct DecoupledTmaCfg {
+// ---------------------------------------------------------------------------
+// Staged (bulk-copy) variant: large tiles live in a ring of shared-memory
+// stages; the tile is reduced from shared memory, its aggregate published,
+// and it is scanned from shared memory once its prefix is known. Roles:
+//   warp 0          producer: tickets + cp.async.bulk of whole tiles;
+//   warp 1          look-back: tile aggregate, publish, look-back, prefix;
+//   warps 2..NC+1   compute: reduce pass of tile k+1 while the look-back of
+//                   tile k is in flight, then the scan pass of tile k with
+//                   coalesced 16-byte streaming stores.
+// Hand-offs use mbarriers only (no CTA-wide barrier inside the loop), and
+// every wait is bounded, so a timeout anywhere lets every warp leave.
+template <class Pol>
+struct pol_commutative : std::false_type {};
+template <class T, class Op>
+struct pol_commutative<PlainScan<T, Op>>
+    : std::bool_constant<std::is_same_v<Op, plus> || std::is_same_v<Op, multiplies> ||
+                         std::is_same_v<Op, bit_and> || std::is_same_v<Op, bit_or> ||
+                         std::is_same_v<Op, bit_xor> || std::is_same_v<Op, minimum> ||
+                         std::is_same_v<Op, maximum>> {};
+template <>
+struct pol_commutative<CompensatedF32> : std::true_type {};
+template <>
+struct pol_commutative<F64CarryF32> : std::true_type {};
+
+template <class Pol, int NC_, int CH_, int STAGES_, int LBW_>
+struct StagedCfg {
   using in_t = typename Pol::in_t;
   using acc_t = typename Pol::acc_t;
   using carry_t = typename Pol::carry_t;
-  static constexpr int NC = NC_;
-  static constexpr int CH = CH_;
-  static constexpr int STAGES = STAGES_;
-  static_assert(16 % sizeof(in_t) == 0, "TMA path needs element sizes dividing 16 bytes");
+  static constexpr int NC = NC_;            // compute warps
+  static constexpr int CH = CH_;            // 16-byte chunks per lane per segment
+  static constexpr int STAGES = STAGES_;    // shared-memory ring depth
+  static constexpr int LBW = LBW_;          // look-back windows (of 32 tiles) per round trip
+  static_assert(16 % sizeof(in_t) == 0, "staged path needs element sizes dividing 16 bytes");
   static constexpr int V = 16 / sizeof(in_t);
-  static constexpr int WARP_ELEMS = 32 * CH * V;
-  static constexpr int TILE = NC * WARP_ELEMS;
+  static constexpr int SEG = 32 * CH * V;   // elements per compute warp
+  static constexpr int TILE = NC * SEG;
   static constexpr int TILE_BYTES = TILE * int(sizeof(in_t));
-  static constexpr int THREADS = (NC + 1) * 32;
-  static constexpr size_t OFF_BAR = size_t(STAGES) * TILE_BYTES;
-  static constexpr size_t OFF_TILE = OFF_BAR + 2 * STAGES * 8;
-  static constexpr size_t OFF_WTOT = align_up(OFF_TILE + STAGES * 8, 16);
-  static constexpr size_t OFF_WPREF = align_up(OFF_WTOT + NC * sizeof(acc_t), 16);
-  static constexpr size_t OFF_FLAG = align_up(OFF_WPREF + NC * sizeof(carry_t), 16);
-  static constexpr size_t SMEM = OFF_FLAG + 16;
-  static_assert(NC <= 32, "at most 32 consumer warps");
+  static constexpr int THREADS = (NC + 2) * 32;
+  // per-stage metadata
+  static constexpr size_t META_AGG = 0;                                   // acc_t[NC] segment aggregates
+  static constexpr size_t META_PREF = align_up(NC * sizeof(acc_t), 16);   // carry_t tile exclusive prefix
+  static constexpr size_t META_TAGG = META_PREF + align_up(sizeof(carry_t), 16);  // carry_t tile aggregate
+  static constexpr size_t META_TILE = META_TAGG + align_up(sizeof(carry_t), 8);   // long long tile index
+  static constexpr size_t META_CNT = META_TILE + 8;                                // unsigned arrivals
+  static constexpr size_t META_BYTES = align_up(META_CNT + 4, 16);
+  static constexpr size_t OFF_META = size_t(STAGES) * TILE_BYTES;
+  static constexpr size_t OFF_BAR = align_up(OFF_META + STAGES * META_BYTES, 8);  // 4 barriers / stage
+  static constexpr size_t SMEM = OFF_BAR + 4 * STAGES * 8;
 };
 
-template <class Pol, int NC, int CH, int STAGES>
-__global__ void __launch_bounds__((NC + 1) * 32)
-    decoupled_tma_kernel(const ScanArgs args) {
-  using Cfg = DecoupledTmaCfg<Pol, NC, CH, STAGES>;
+// Warp-wide look-back reading LBW windows of 32 descriptors per round trip.
+template <class Pol, int LBW>
+__device__ __forceinline__ bool lookback_multi(const Pol& pol, const uint64_t* desc, long long tile,
+                                               uint32_t etag, WsHeader* hdr, uint64_t timeout_ns, int lane,
+                                               typename Pol::carry_t& out, unsigned long long& stats) {
+  unsigned rounds = 0, spin_total = 0;
+  using C = typename Pol::carry_t;
+  using codec = desc_codec<C>;
+  auto cop = [&](const C& x, const C& y) { return pol.cop(x, y); };
+  C acc = pol.cid();
+  long long base = tile - 1;
+  uint32_t spins = 0;
+  uint64_t t0 = 0;
+  while (true) {
+    C v[LBW];
+    uint32_t st[LBW];
+#pragma unroll
+    for (int j = 0; j < LBW; ++j) {
+      const long long t = base - lane - 32 * j;
+      v[j] = pol.cid();
+      st[j] = kPrefix;
+      if (t >= 0) st[j] = codec::read(desc + t * codec::W, etag, v[j]);
+    }
+    // nearest inclusive prefix: first window with one, lowest lane in it
+    int pj = LBW, pl = 32;
+    bool blocked = false;
+#pragma unroll
+    for (int j = 0; j < LBW; ++j) {
+      const uint32_t pm = __ballot_sync(kFullMask, st[j] == kPrefix);
+      const uint32_t xm = __ballot_sync(kFullMask, st[j] == kInvalid);
+      if (pj == LBW) {
+        if (pm) {
+          const int p = __ffs(pm) - 1;
+          const uint32_t need = (p >= 31) ? kFullMask : ((2u << p) - 1u);
+          blocked |= (xm & need) != 0u;
+          pj = j;
+          pl = p;
+        } else {
+          blocked |= xm != 0u;
+        }
+      }
+    }
+    if (blocked) {
+      if (spins == 0) t0 = ptx::globaltimer_ns();
+      ++spins;
+      ++spin_total;
+      if ((spins & 7u) == 0u) {
+        bool give_up = false;
+        if (lane == 0) {
+          if (aborted(hdr)) {
+            give_up = true;
+          } else if (ptx::globaltimer_ns() - t0 > timeout_ns) {
+            raise_error(hdr, kDevTimeout, (unsigned long long)tile);
+            give_up = true;
+          }
+        }
+        if (__shfl_sync(kFullMask, give_up, 0)) return false;
+      }
+      continue;
+    }
+    spins = 0;
+    ++rounds;
+    // fold windows newest -> oldest: acc = older op acc
+#pragma unroll
+    for (int j = 0; j < LBW; ++j) {
+      if (j <= pj) {
+        C w = (j < pj || lane <= pl) ? v[j] : pol.cid();
+        w = warp_reduce_reversed(w, cop, lane);
+        acc = pol.cop(w, acc);
+      }
+    }
+    if (pj < LBW) break;
+    base -= 32 * LBW;
+  }
+  out = acc;
+  stats = (unsigned long long)rounds | ((unsigned long long)spin_total << 32);
+  return true;
+}
+
+template <class Pol, int NC, int CH, int STAGES, int LBW, class Trace = NoTrace>
+__global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(const ScanArgs args) {
+  using Cfg = StagedCfg<Pol, NC, CH, STAGES, LBW>;
   using in_t = typename Pol::in_t;
   using out_t = typename Pol::out_t;
   using acc_t = typename Pol::acc_t;
   using carry_t = typename Pol::carry_t;
   using pre_t = typename Pol::pre_t;
-  using TS = TileScan<Pol, NC, CH, Cfg::V>;
+  using codec = desc_codec<carry_t>;
   constexpr int V = Cfg::V;
   constexpr int TILE = Cfg::TILE;
   static_assert(sizeof(out_t) == sizeof(in_t), "in/out element sizes must match");
 
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + Cfg::OFF_BAR);
-  uint64_t* empty = full + STAGES;
-  long long* s_tile = reinterpret_cast<long long*>(smem + Cfg::OFF_TILE);
-  acc_t* s_wtot = reinterpret_cast<acc_t*>(smem + Cfg::OFF_WTOT);
-  carry_t* s_wpref = reinterpret_cast<carry_t*>(smem + Cfg::OFF_WPREF);
-  int* s_flag = reinterpret_cast<int*>(smem + Cfg::OFF_FLAG);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + Cfg::OFF_BAR);
+  uint64_t* full = bars;
+  uint64_t* empty = bars + STAGES;
+  uint64_t* aggb = bars + 2 * STAGES;
+  uint64_t* prefb = bars + 3 * STAGES;
+  auto meta = [&](int s) { return smem + Cfg::OFF_META + size_t(s) * Cfg::META_BYTES; };
+  auto s_aggs = [&](int s) { return reinterpret_cast<acc_t*>(meta(s) + Cfg::META_AGG); };
+  auto s_pref = [&](int s) { return reinterpret_cast<carry_t*>(meta(s) + Cfg::META_PREF); };
+  auto s_tagg = [&](int s) { return reinterpret_cast<carry_t*>(meta(s) + Cfg::META_TAGG); };
+  auto s_tile = [&](int s) { return reinterpret_cast<long long*>(meta(s) + Cfg::META_TILE); };
+  auto s_cnt = [&](int s) { return reinterpret_cast<unsigned*>(meta(s) + Cfg::META_CNT); };
 
   const Pol pol{};
+  const Trace trace{};
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const uint64_t n = args.n;
   const long long ntiles = (long long)((n + TILE - 1) / TILE);
   WsHeader* hdr = args.hdr;
+  const uint64_t tmo = args.timeout_ns;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       ptx::mbar_init(&full[s], 1);
       ptx::mbar_init(&empty[s], NC);
+      ptx::mbar_init(&aggb[s], NC);
+      ptx::mbar_init(&prefb[s], 1);
+      *s_cnt(s) = 0u;
     }
     ptx::fence_mbar_init();
   }
   __syncthreads();
+  const uint32_t etag = ptx::ld_relaxed(reinterpret_cast<const uint32_t*>(&hdr->epoch)) + 1u;
 
   if (warp == 0) {
-    // ---------------- producer ----------------
+    // ------------------------------------------------------------ producer
     if (lane == 0) {
       const uint64_t pol_l2 = ptx::policy_evict_first();
       const unsigned char* in = static_cast<const unsigned char*>(args.in);
-      uint32_t pending = 0;  // stages whose last copy may still be in flight
-      uint32_t pend_par = 0;
+      uint32_t pending = 0, pend_par = 0;
       long long t = (long long)atomicAdd(&hdr->ticket, 1ull);
       for (int k = 0;; ++k) {
         const int s = k % STAGES;
         if (k >= STAGES) {
-          if (!mbar_wait_bounded(&empty[s], ((k / STAGES) - 1) & 1, hdr, args.timeout_ns, (unsigned long long)t))
-            break;
+          if (!mbar_wait_bounded(&empty[s], ((k / STAGES) - 1) & 1, hdr, tmo, (unsigned long long)t)) break;
           pending &= ~(1u << s);
         }
-        s_tile[s] = t;
+        *s_tile(s) = t;
         if (t < ntiles) {
           const uint64_t base = uint64_t(t) * TILE;
           const uint64_t valid = (n - base < uint64_t(TILE)) ? (n - base) : uint64_t(TILE);
@@ -280,84 +417,178 @@ __global__ void __launch_bounds__((NC + 1) * 32)
           break;
         }
       }
-      // never leave with a bulk copy still writing into this CTA's shared memory
       for (int s = 0; s < STAGES; ++s)
-        if (pending & (1u << s)) mbar_wait_bounded(&full[s], (pend_par >> s) & 1u, hdr, args.timeout_ns, 0ull);
+        if (pending & (1u << s)) mbar_wait_bounded(&full[s], (pend_par >> s) & 1u, hdr, tmo, 0ull);
     }
     __syncwarp();
-  } else {
-    // ---------------- consumers ----------------
-    const int cw = warp - 1;
-    const uint32_t etag = ptx::ld_relaxed(reinterpret_cast<const uint32_t*>(&hdr->epoch)) + 1u;
-    const in_t* gin = static_cast<const in_t*>(args.in);
-    out_t* gout = static_cast<out_t*>(args.out);
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ look-back
     for (int k = 0;; ++k) {
       const int s = k % STAGES;
-      // A warp whose wait gave up (timeout / abort) and the end-of-work
-      // sentinel both make the warp inactive; the OR-vote at the first named
-      // barrier lets every consumer warp leave the loop together.
-      const bool got = mbar_wait_bounded(&full[s], (k / STAGES) & 1, hdr, args.timeout_ns, 0ull);
-      const long long tile = got ? s_tile[s] : ntiles;
-      const bool active = tile < ntiles;
-
+      const uint32_t par = (k / STAGES) & 1;
+      if (!mbar_wait_bounded(&full[s], par, hdr, tmo, 0ull)) break;
+      const long long tile = *s_tile(s);
+      if (tile >= ntiles) break;
+      trace(kTrFull, tile, ptx::globaltimer_ns());
       uint32_t peek_st = kInvalid;
       carry_t peek_v = pol.cid();
-      const uint64_t base = uint64_t(active ? tile : 0) * TILE;
+      if (lane == 0 && tile > 0) peek_st = codec::read(args.desc + (tile - 1) * codec::W, etag, peek_v);
+      if (!mbar_wait_bounded(&aggb[s], par, hdr, tmo, 0ull)) break;
+      trace(kTrAgg, tile, ptx::globaltimer_ns());
+      // the tile aggregate was published by the last compute warp of the reduce pass
+      const carry_t agg = *s_tagg(s);
+      uint64_t* d = args.desc + tile * codec::W;
+      const bool publish = tile != args.debug_skip_tile;
+      carry_t excl = pol.cid();
+      bool ok = true;
+      unsigned long long stats = 0;
+      const bool ready = tile == 0 || __shfl_sync(kFullMask, peek_st, 0) == kPrefix;
+      if (tile == 0) {
+        // published as a prefix by the reduce pass
+      } else if (ready) {
+        // reduce-then-scan: predecessor prefix known on arrival
+        excl = shfl_idx(peek_v, 0);
+        if (lane == 0 && publish) codec::publish(d, pol.cop(excl, agg), make_tag(etag, kPrefix));
+      } else {
+        // scan-then-reduce: the aggregate is out, look back for the prefix
+        ok = lookback_multi<Pol, LBW>(pol, args.desc, tile, etag, hdr, tmo, lane, excl, stats);
+        if (ok && lane == 0 && publish) codec::publish(d, pol.cop(excl, agg), make_tag(etag, kPrefix));
+      }
+      if (!ok) break;
+      trace(kTrLbDone, tile, ptx::globaltimer_ns());
+      trace(kTrLbRounds, tile, stats);
+      trace(kTrPeek, tile, ready ? 1ull : 0ull);
+      if (lane == 0) {
+        *s_pref(s) = excl;
+        ptx::mbar_arrive(&prefb[s]);
+      }
+      __syncwarp();
+    }
+  } else {
+    // ------------------------------------------------------------ compute
+    const int w = warp - 2;
+    const in_t* gin = static_cast<const in_t*>(args.in);
+    out_t* gout = static_cast<out_t*>(args.out);
+    const bool excl_kind = args.exclusive != 0;
+    auto aop = [&](const acc_t& x, const acc_t& y) { return pol.aop(x, y); };
+
+    // chunk c of this lane: V elements at tile offset w*SEG + (c*32 + lane)*V
+    auto load_chunk = [&](int s, int c, uint64_t base, int valid, int bulk, acc_t (&a)[V]) {
+      const unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
+      const int e0 = w * Cfg::SEG + (c * 32 + lane) * V;
+      if (e0 + V <= bulk) {
+        union {
+          uint4 u;
+          in_t x[V];
+        } buf;
+        buf.u = *reinterpret_cast<const uint4*>(stage + size_t(e0) * sizeof(in_t));
+#pragma unroll
+        for (int j = 0; j < V; ++j) a[j] = pol.load(buf.x[j]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < V; ++j) {
+          const int e = e0 + j;
+          if (e < bulk)
+            a[j] = pol.load(reinterpret_cast<const in_t*>(stage)[e]);
+          else if (e < valid)
+            a[j] = pol.load(gin[base + e]);
+          else
+            a[j] = pol.aid();
+        }
+      }
+    };
+    // reduce pass of use k: returns false at the end of work or on a failed wait
+    auto reduce_pass = [&](int k) -> bool {
+      const int s = k % STAGES;
+      if (!mbar_wait_bounded(&full[s], (k / STAGES) & 1, hdr, tmo, 0ull)) return false;
+      const long long tile = *s_tile(s);
+      if (tile >= ntiles) return false;
+      const uint64_t base = uint64_t(tile) * TILE;
       const uint64_t rem = n - base;
       const int valid = rem < uint64_t(TILE) ? int(rem) : TILE;
-      acc_t a[CH][V];
-      acc_t pre_lane[CH];
-      if (active) {
-        if (cw == 0 && lane == 0 && tile > 0)
-          peek_st = TS::codec::read(args.desc + (tile - 1) * TS::codec::W, etag, peek_v);
-        const int bulk_elems = int((uint32_t(valid * sizeof(in_t)) & ~15u) / sizeof(in_t));
-        const unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
-#pragma unroll
+      const int bulk = int((uint32_t(valid * sizeof(in_t)) & ~15u) / sizeof(in_t));
+      acc_t r = pol.aid();
+      if constexpr (pol_commutative<Pol>::value) {
+#pragma unroll 4
         for (int c = 0; c < CH; ++c) {
-          const int e0 = cw * Cfg::WARP_ELEMS + (c * 32 + lane) * V;
-          if (e0 + V <= bulk_elems) {
-            union {
-              uint4 u;
-              in_t x[V];
-            } buf;
-            buf.u = *reinterpret_cast<const uint4*>(stage + size_t(e0) * sizeof(in_t));
+          acc_t a[V];
+          load_chunk(s, c, base, valid, bulk, a);
 #pragma unroll
-            for (int j = 0; j < V; ++j) a[c][j] = pol.load(buf.x[j]);
-          } else {
-#pragma unroll
-            for (int j = 0; j < V; ++j) {
-              const int e = e0 + j;
-              if (e < bulk_elems)
-                a[c][j] = pol.load(reinterpret_cast<const in_t*>(stage)[e]);
-              else if (e < valid)
-                a[c][j] = pol.load(gin[base + e]);
-              else
-                a[c][j] = pol.aid();
-            }
-          }
+          for (int j = 0; j < V; ++j) r = pol.aop(r, a[j]);
         }
-        __syncwarp();
-        if (lane == 0) ptx::mbar_arrive(&empty[s]);  // stage may be refilled
-
-        const acc_t wagg = TS::warp_part(pol, a, pre_lane, lane);
-        if (lane == 0) s_wtot[cw] = wagg;
-      }
-      if (ptx::named_sync_or(1, NC * 32, !active)) break;
-      if (cw == 0) TS::resolve(pol, args, tile, etag, s_wtot, s_wpref, s_flag, peek_st, peek_v, lane);
-      ptx::named_sync(1, NC * 32);
-      if (*s_flag) break;
-
-      const pre_t pw = pol.prepare(s_wpref[cw]);
-      const bool excl = args.exclusive != 0;
+        r = warp_reduce(r, aop, lane);
+      } else {
+        for (int c = 0; c < CH; ++c) {
+          acc_t a[V];
+          load_chunk(s, c, base, valid, bulk, a);
+          acc_t t = a[0];
 #pragma unroll
+          for (int j = 1; j < V; ++j) t = pol.aop(t, a[j]);
+          r = pol.aop(r, warp_reduce(t, aop, lane));
+        }
+      }
+      // the last compute warp to finish combines the segment aggregates and
+      // publishes the tile aggregate at once (tile 0: its inclusive prefix),
+      // so successors never wait for this CTA's look-back of an earlier tile
+      unsigned last = 0;
+      if (lane == 0) {
+        s_aggs(s)[w] = r;
+        __threadfence_block();
+        last = atomicAdd(s_cnt(s), 1u) == unsigned(NC - 1);
+      }
+      if (__shfl_sync(kFullMask, last, 0)) {
+        __threadfence_block();
+        acc_t x = lane < NC ? s_aggs(s)[lane] : pol.aid();
+        x = warp_inclusive_scan(x, aop, lane);
+        const carry_t agg = pol.to_carry(shfl_idx(x, NC - 1));
+        if (lane == 0) {
+          *s_tagg(s) = agg;
+          *s_cnt(s) = 0u;
+          if (tile != args.debug_skip_tile)
+            codec::publish(args.desc + tile * codec::W, agg, make_tag(etag, tile == 0 ? kPrefix : kAggregate));
+          trace(kTrAggPub, tile, ptx::globaltimer_ns());
+        }
+      }
+      __syncwarp();
+      if (lane == 0) ptx::mbar_arrive(&aggb[s]);
+      __syncwarp();
+      return true;
+    };
+
+    bool have = reduce_pass(0);
+    for (int k = 0; have; ++k) {
+      const bool have_next = reduce_pass(k + 1);
+      // scan pass of use k
+      const int s = k % STAGES;
+      if (!mbar_wait_bounded(&prefb[s], (k / STAGES) & 1, hdr, tmo, 0ull)) break;
+      const long long tile = *s_tile(s);
+      if (w == 0 && lane == 0) trace(kTrSStart, tile, ptx::globaltimer_ns());
+      const uint64_t base = uint64_t(tile) * TILE;
+      const uint64_t rem = n - base;
+      const int valid = rem < uint64_t(TILE) ? int(rem) : TILE;
+      const int bulk = int((uint32_t(valid * sizeof(in_t)) & ~15u) / sizeof(in_t));
+      // exclusive prefix of this warp's segment inside the tile
+      acc_t sx = (lane < w) ? s_aggs(s)[lane] : pol.aid();
+      sx = warp_reduce(sx, aop, lane);
+      const pre_t pw = pol.prepare(w == 0 ? *s_pref(s) : pol.cop(*s_pref(s), pol.to_carry(sx)));
+      acc_t X = pol.aid();
+#pragma unroll 2
       for (int c = 0; c < CH; ++c) {
-        const int e0 = cw * Cfg::WARP_ELEMS + (c * 32 + lane) * V;
-        const pre_t pc = pol.extend(pw, pre_lane[c]);
+        acc_t a[V];
+        load_chunk(s, c, base, valid, bulk, a);
+#pragma unroll
+        for (int j = 1; j < V; ++j) a[j] = pol.aop(a[j - 1], a[j]);
+        const acc_t inc = warp_inclusive_scan(a[V - 1], aop, lane);
+        acc_t ex = shfl_up(inc, 1);
+        if (lane == 0) ex = pol.aid();
+        const pre_t pc = pol.extend(pw, c == 0 ? ex : pol.aop(X, ex));
+        X = (c == 0) ? shfl_idx(inc, 31) : pol.aop(X, shfl_idx(inc, 31));
         union {
           uint4 u;
           out_t x[V];
         } o;
-        TS::finish_chunk(pol, pc, a[c], excl, o.x);
+        TileScan<Pol, NC, CH, V>::finish_chunk(pol, pc, a, excl_kind, o.x);
+        const int e0 = w * Cfg::SEG + (c * 32 + lane) * V;
         if (e0 + V <= valid) {
           ptx::st_stream_v4(gout + base + e0, o.u);
         } else {
@@ -366,10 +597,16 @@ __global__ void __launch_bounds__((NC + 1) * 32)
             if (e0 + j < valid) gout[base + e0 + j] = o.x[j];
         }
       }
+      __syncwarp();
+      if (lane == 0) {
+        if (w == 0) trace(kTrSDone, tile, ptx::globaltimer_ns());
+        ptx::mbar_arrive(&empty[s]);
+      }
+      have = have_next;
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) cta_exit_rearm(hdr, args.desc, uint64_t(ntiles) * TS::codec::W);
+  if (threadIdx.x == 0) cta_exit_rearm(hdr, args.desc, uint64_t(ntiles) * codec::W);
 }
 
 // ---------------------------------------------------------------------------

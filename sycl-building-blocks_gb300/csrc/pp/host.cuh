@@ -200,12 +200,16 @@ inline Status prepare_kernel(K kernel, int threads, size_t smem, int& blocks_per
 // Decoupled look-back scan.
 template <class Pol>
 struct DecoupledTuning {
-  static constexpr int NC = 8;      // consumer warps
-  static constexpr int CH = 4;      // 16-byte chunks per thread per tile
+  static constexpr int NC = 16;     // compute warps
+  static constexpr int CH = 8;      // 16-byte chunks per lane per segment (64 KB tiles)
   static constexpr int STAGES = 3;  // shared-memory ring depth
+  static constexpr int LBW = 4;     // look-back windows of 32 tiles per round trip
   static constexpr int GEN_NC = 8;
   static constexpr int GEN_IPT = 8;
 };
+template <class Pol>
+using StagedFor = StagedCfg<Pol, DecoupledTuning<Pol>::NC, DecoupledTuning<Pol>::CH, DecoupledTuning<Pol>::STAGES,
+                            DecoupledTuning<Pol>::LBW>;
 
 template <class Pol>
 inline bool tma_path_ok(const void* in, const void* out) {
@@ -221,7 +225,7 @@ template <class Pol>
 inline uint64_t decoupled_tile_elems(const void* in, const void* out) {
   using Tn = DecoupledTuning<Pol>;
   if constexpr (16 % sizeof(typename Pol::in_t) == 0) {
-    if (tma_path_ok<Pol>(in, out)) return DecoupledTmaCfg<Pol, Tn::NC, Tn::CH, Tn::STAGES>::TILE;
+    if (tma_path_ok<Pol>(in, out)) return StagedFor<Pol>::TILE;
   }
   return DecoupledGenericCfg<Pol, Tn::GEN_NC, Tn::GEN_IPT>::TILE;
 }
@@ -259,8 +263,8 @@ inline Status decoupled_scan(cudaStream_t s, const void* in, void* out, uint64_t
   const int cap = grid_ctas > 0 ? grid_ctas : settings().max_ctas.load();
   if constexpr (16 % sizeof(typename Pol::in_t) == 0) {
     if (tma_path_ok<Pol>(in, out)) {
-      using Cfg = DecoupledTmaCfg<Pol, Tn::NC, Tn::CH, Tn::STAGES>;
-      auto k = decoupled_tma_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES>;
+      using Cfg = StagedFor<Pol>;
+      auto k = decoupled_staged_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW>;
       int bps = 0;
       st = prepare_kernel(k, Cfg::THREADS, Cfg::SMEM, bps);
       if (st != Status::ok) return st;

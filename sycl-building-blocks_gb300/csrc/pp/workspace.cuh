@@ -18,8 +18,11 @@
 // invalid. A value wider than 32 bits is split over 2 or 4 words that all
 // carry the tag; a reader accepts a descriptor only when every word carries
 // the same current-epoch tag, so a half-updated descriptor reads as invalid.
-// Every word is written with one st.relaxed.gpu and read with ld.relaxed.gpu:
-// the payload travels with its flag, so no fence is needed on either side.
+// Every word is published with one 64-bit atomic max (red.max: the tag sits in
+// the high bits, so within an epoch a word can only move invalid -> aggregate
+// -> prefix, whatever order two publishers' writes land in) and read with
+// ld.relaxed.gpu: the payload travels with its flag, so no fence is needed on
+// either side.
 //
 // The epoch removes the per-call descriptor fill of the reference
 // (scan_decoupled_lookback.hpp:115-116): the last CTA of every launch bumps
@@ -80,7 +83,7 @@ struct desc_codec {
 #pragma unroll
     for (int i = 0; i < W; ++i) {
       const uint32_t w = i < PW ? p.w[i < PW ? i : 0] : 0u;
-      ptx::st_relaxed(d + i, hi | w);
+      atomicMax(reinterpret_cast<unsigned long long*>(d + i), (unsigned long long)(hi | w));
     }
   }
 

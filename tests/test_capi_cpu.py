@@ -57,11 +57,13 @@ def test_status_strings_and_version(pp):
 
 
 def test_workspace_size_is_host_only(pp):
-    # 2^30 uint32 on the aligned (bulk-copy) path: 4096-element tiles, one descriptor word each
+    # 2^30 uint32 on the aligned (bulk-copy) path: 64 KB tiles, one descriptor word each
     a = 1 << 12
     n = 1 << 30
     size = pp.workspace_size("decoupled", "u32", a, a, n)
-    assert size == 4096 + 8192 * 16 + (n // 4096) * 8
-    # uint64: 2048-element tiles, two words each
-    assert pp.workspace_size("decoupled", "u64", a, a, n) == 4096 + 8192 * 16 + (n // 2048) * 16
+    assert size == 4096 + 8192 * 16 + (n // 16384) * 8
+    # uint64: 64 KB tiles, two words each
+    assert pp.workspace_size("decoupled", "u64", a, a, n) == 4096 + 8192 * 16 + (n // 8192) * 16
+    # unaligned pointers take the generic kernel: 2048-element register tiles
+    assert pp.workspace_size("decoupled", "u32", a + 4, a, n) == 4096 + 8192 * 16 + (n // 2048) * 8
     assert pp.workspace_size("cooperative", "f32", a, a, n) == 4096 + 8192 * 16

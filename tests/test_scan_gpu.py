@@ -14,10 +14,12 @@ from helpers import (FLOAT_DTYPES, FLOAT_OPS, INT_DTYPES, INT_OPS, NP, check_sca
 
 pytestmark = pytest.mark.gpu
 
-# sizes around the tile edges of both kernels (TMA tile: 4096 x 4-byte or
-# 2048 x 8-byte elements; generic tile: 2048 elements), ragged tails and
-# lengths whose byte count is not a multiple of 16
-SIZES = [1, 2, 3, 31, 32, 33, 2047, 2048, 2049, 4095, 4096, 4097, 12289, 65537, 1000003]
+# sizes around the tile edges of both kernels (staged tile: 64 KB = 16384 x
+# 4-byte or 8192 x 8-byte elements, compute-warp segments of 1024 / 512;
+# generic tile: 2048 elements), ragged tails and lengths whose byte count is
+# not a multiple of 16
+SIZES = [1, 2, 3, 31, 32, 33, 511, 513, 1023, 1025, 2047, 2048, 2049, 8191, 8192, 8193, 16383, 16384, 16385,
+         49153, 65537, 1000003]
 ALL = [(d, o) for d in INT_DTYPES for o in INT_OPS] + [(d, o) for d in FLOAT_DTYPES for o in FLOAT_OPS]
 
 
