@@ -28,6 +28,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -347,7 +348,132 @@ def run_secondary(torch, pp, stream, args, d_in32, d_out32) -> dict:
     out["f32_reduce_check"] = {"sum": float(r[0]), "fp64_sum": ref_sum, "abs_err": abs(float(r[0]) - ref_sum),
                                "max_exact": float(r[1]) == ref_max}
     del f
+    out["precision_f32_2p28"] = bench_precision(torch, pp, stream, steps, gen)
+    out["segmented_2p16_segments"] = bench_segmented(torch, pp, stream, steps)
+    out["cumsum_4096x8192"] = bench_cumsum(torch, stream, steps)
     return out
+
+
+def _err_stats(torch, got, ref):
+    """max / RMS relative error per prefix (prefixes with |s| >= 1e-3 rms(s))
+    and the normwise error max|err| / max|s|, against an FP64 scan."""
+    err = (got.double() - ref).abs()
+    scale = torch.sqrt(torch.mean(ref * ref))
+    mask = ref.abs() >= 1e-3 * scale
+    rel = err[mask] / ref.abs()[mask]
+    return {"max_rel": float(rel.max()), "rms_rel": float(torch.sqrt(torch.mean(rel * rel))),
+            "normwise": float(err.max() / ref.abs().max()), "excluded_near_zero": int((~mask).sum())}
+
+
+def bench_precision(torch, pp, stream, steps, gen) -> dict:
+    """f32 plus-scan of 2^28 N(0,1) and sign-random lognormal(0, 2) values:
+    plain, compensated and FP64-carry, GB/s and errors vs an FP64 scan."""
+    sh = stream.cuda_stream
+    n = 1 << 28
+    res = {}
+    out = torch.empty(n, dtype=torch.float32, device="cuda")
+    for dist in ("normal", "lognormal"):
+        x = torch.randn(n, dtype=torch.float32, device="cuda", generator=gen)
+        if dist == "lognormal":
+            sign = torch.randint(0, 2, (n,), device="cuda", generator=gen).float() * 2 - 1
+            x = (torch.exp(2.0 * x) * sign).float()
+        ref = torch.cumsum(x.double(), 0)
+        d = {}
+        for prec in ("default", "compensated", "fp64_carry"):
+            fn = lambda p=prec: pp.scan("inclusive", "plus", x.data_ptr(), out.data_ptr(), n, "f32", stream=sh,
+                                        precision=p)
+            ms, _ = time_device(torch, fn, steps, 2, stream)
+            if pp.stream_status(sh) != 0:
+                raise RuntimeError("device error in precision benchmark")
+            d[prec] = {"gbs": round(8 * n * steps / (ms * 1e-3) / 1e9, 2), **_err_stats(torch, out, ref)}
+        d["compensated_slowdown_vs_plain"] = round(d["default"]["gbs"] / d["compensated"]["gbs"] - 1, 4)
+        res[dist] = d
+        del x, ref
+    return res
+
+
+def bench_segmented(torch, pp, stream, steps) -> dict:
+    """65,536 segments, lengths floor(exp(U[0, ln 2^16])) clipped to [1, 2^16]
+    (about 2^28 elements), int64 offsets; int32 U[0,1000) and f32 N(0,1)
+    payloads. One batched launch in a CUDA graph vs one launch per segment
+    (also replayed from a CUDA graph)."""
+    S = 65536
+    g = torch.Generator(device="cpu").manual_seed(0x5EC)
+    lens = torch.floor(torch.exp(torch.rand(S, generator=g, dtype=torch.float64) * math.log(2 ** 16)))
+    lens = lens.clamp(1, 2 ** 16).to(torch.int64)
+    offs = torch.zeros(S + 1, dtype=torch.int64)
+    offs[1:] = torch.cumsum(lens, 0)
+    n = int(offs[-1])
+    d_off = offs.cuda()
+    gd = torch.Generator(device="cuda").manual_seed(0x5EC)
+    res = {"segments": S, "elements": n}
+    for dt, make in (("i32", lambda: torch.randint(0, 1000, (n,), dtype=torch.int32, device="cuda", generator=gd)),
+                     ("f32", lambda: torch.randn(n, dtype=torch.float32, device="cuda", generator=gd))):
+        x = make()
+        y = torch.empty_like(x)
+        s = torch.cuda.Stream()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(s):
+            pp.segmented_scan("inclusive", "plus", x.data_ptr(), y.data_ptr(), n, d_off.data_ptr(), S, dt,
+                              stream=s.cuda_stream)
+            s.synchronize()
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph, stream=s):
+                pp.segmented_scan("inclusive", "plus", x.data_ptr(), y.data_ptr(), n, d_off.data_ptr(), S, dt,
+                                  stream=s.cuda_stream)
+        ms_b, _ = time_device(torch, graph.replay, steps, 2, torch.cuda.current_stream())
+        # check a few segments against torch
+        ok = True
+        for k in (0, 1, S // 2, S - 1):
+            a, b = int(offs[k]), int(offs[k + 1])
+            ref = torch.cumsum(x[a:b].double(), 0)
+            ok &= bool(((y[a:b].double() - ref).abs() <= 1e-4 * (1 + ref.abs())).all())
+        # one plain launch per segment, captured once, replayed
+        with torch.cuda.stream(s):
+            big = int(lens.max())
+            pp.decoupled_scan_device("inclusive", "plus", x.data_ptr(), y.data_ptr(), big, dt, stream=s.cuda_stream)
+            s.synchronize()
+            graph2 = torch.cuda.CUDAGraph()
+            esz = x.element_size()
+            offl = offs.tolist()
+            with torch.cuda.graph(graph2, stream=s):
+                for k in range(S):
+                    a, b = offl[k], offl[k + 1]
+                    pp.decoupled_scan_device("inclusive", "plus", x.data_ptr() + a * esz, y.data_ptr() + a * esz,
+                                             b - a, dt, stream=s.cuda_stream)
+        ms_p, _ = time_device(torch, graph2.replay, max(2, steps // 20), 1, torch.cuda.current_stream())
+        if pp.stream_status(s.cuda_stream) != 0:
+            raise RuntimeError("device error in segmented benchmark")
+        res[dt] = {"batched_elems_per_s": round(n / (ms_b * 1e-3), 1), "batched_ms": round(ms_b / steps, 4),
+                   "per_segment_launches_ms": round(ms_p / max(2, steps // 20), 3),
+                   "speedup": round((ms_p / max(2, steps // 20)) / (ms_b / steps), 2),
+                   "batched_gbs": round(2 * n * 4 / (ms_b / steps * 1e-3) / 1e9, 2), "spot_check": ok}
+        del graph, graph2, x, y
+    return res
+
+
+def bench_cumsum(torch, stream, steps) -> dict:
+    """Differentiable cumsum of a 4096 x 8192 f32 N(0,1) tensor through the
+    libtorch binding: forward + backward GB/s (2 * B * L * 4 bytes each)."""
+    try:
+        import ppcumsum
+
+        ext = ppcumsum.load()
+    except Exception as e:  # the optional binding needs a torch build toolchain
+        return {"unavailable": str(e)[:200]}
+    g = torch.Generator(device="cuda").manual_seed(5)
+    x = torch.randn(4096, 8192, device="cuda", generator=g).requires_grad_(True)
+    up = torch.randn(4096, 8192, device="cuda", generator=g)
+
+    def step():
+        x.grad = None
+        ext.cumsum(x).backward(up)
+
+    ms, _ = time_device(torch, step, steps, 2, torch.cuda.current_stream())
+    nbytes = 2 * (2 * 4096 * 8192 * 4)
+    ref = torch.flip(torch.cumsum(torch.flip(up.double(), [1]), 1), [1])
+    return {"fwd_bwd_gbs": round(nbytes * steps / (ms * 1e-3) / 1e9, 2), "ms_per_fwd_bwd": round(ms / steps, 4),
+            "grad_max_abs_err": float((x.grad.double() - ref).abs().max())}
 
 
 # ---------------------------------------------------------------------------------

@@ -131,6 +131,27 @@ pp_status pp_cooperative_scan_host(pp_scan_kind kind, pp_op op, pp_dtype dtype, 
 pp_status pp_scan_host(pp_scan_kind kind, pp_op op, pp_dtype dtype, const void* h_in, void* h_out, uint64_t n);
 pp_status pp_reduce_host(pp_op op, pp_dtype dtype, const void* h_in, uint64_t n, void* h_result);
 
+/* ---- batched segmented scans and reductions ---------------------------------
+ * No counterpart in the reference (it scans one array per call). Segments are
+ * given in CSR form: d_offsets holds num_segments + 1 int64 entries,
+ * offsets[0] = 0, offsets[num_segments] = n, nondecreasing; segment s is
+ * elements [offsets[s], offsets[s+1]). All segments run in one persistent
+ * scan launch (after a small head-flag pre-pass), so the call is
+ * CUDA-graph-capturable once the stream's workspace has been sized by an
+ * earlier call with the same or larger n. Operators: plus, minimum, maximum.
+ * Data pointers must be 16-byte aligned (PP_ERR_INVALID_ARG otherwise). */
+pp_status pp_segmented_scan(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dtype, const void* d_in,
+                            void* d_out, uint64_t n, const int64_t* d_offsets, uint64_t num_segments);
+/* d_out[s] = reduction of segment s (the operator's identity for an empty one). */
+pp_status pp_segmented_reduce(pp_stream stream, pp_op op, pp_dtype dtype, const void* d_in, uint64_t n,
+                              const int64_t* d_offsets, uint64_t num_segments, void* d_out);
+/* Scan every row of a rows x cols row-major matrix independently (a batched
+ * cumsum along the last dimension); reverse != 0 gives suffix scans
+ * (out[r][c] = in[r][c] op ... op in[r][cols-1]), the adjoint of a prefix
+ * sum. */
+pp_status pp_rows_scan(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dtype, const void* d_in, void* d_out,
+                       uint64_t rows, uint64_t cols, int reverse);
+
 /* ---- status / settings ----------------------------------------------------- */
 
 const char* pp_status_string(pp_status status);
@@ -152,6 +173,7 @@ pp_status pp_debug_set_skip_tile(long long tile);
 
 /* Library version string. */
 const char* pp_version(void);
+
 
 #ifdef __cplusplus
 }

@@ -329,6 +329,81 @@ pp_status pp_debug_set_skip_tile(long long tile) {
   return PP_OK;
 }
 
+namespace {
+Status seg_dispatch(const pp::capi::SegReq& r, pp_dtype dt, int which) {
+  using namespace pp::capi;
+  switch (dt) {
+    case PP_I32:
+      return which == 0 ? seg_scan_typed<int32_t>(r) : which == 1 ? seg_reduce_typed<int32_t>(r) : rows_scan_typed<int32_t>(r);
+    case PP_U32:
+      return which == 0 ? seg_scan_typed<uint32_t>(r) : which == 1 ? seg_reduce_typed<uint32_t>(r) : rows_scan_typed<uint32_t>(r);
+    case PP_I64:
+      return which == 0 ? seg_scan_typed<int64_t>(r) : which == 1 ? seg_reduce_typed<int64_t>(r) : rows_scan_typed<int64_t>(r);
+    case PP_U64:
+      return which == 0 ? seg_scan_typed<uint64_t>(r) : which == 1 ? seg_reduce_typed<uint64_t>(r) : rows_scan_typed<uint64_t>(r);
+    case PP_F32:
+      return which == 0 ? seg_scan_typed<float>(r) : which == 1 ? seg_reduce_typed<float>(r) : rows_scan_typed<float>(r);
+    case PP_F64:
+      return which == 0 ? seg_scan_typed<double>(r) : which == 1 ? seg_reduce_typed<double>(r) : rows_scan_typed<double>(r);
+  }
+  return Status::invalid_arg;
+}
+bool valid_seg_op(pp_op op) { return op == PP_OP_PLUS || op == PP_OP_MINIMUM || op == PP_OP_MAXIMUM; }
+}  // namespace
+
+pp_status pp_segmented_scan(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dtype, const void* d_in,
+                            void* d_out, uint64_t n, const int64_t* d_offsets, uint64_t num_segments) {
+  if (!valid_kind(kind) || !valid_op(op) || !valid_dtype(dtype)) return PP_ERR_INVALID_ARG;
+  if (!valid_seg_op(op)) return PP_ERR_UNSUPPORTED;
+  if (n == 0 || num_segments == 0) return PP_OK;
+  if (!d_in || !d_out || !d_offsets) return PP_ERR_INVALID_ARG;
+  pp::capi::SegReq r;
+  r.s = static_cast<cudaStream_t>(stream);
+  r.exclusive = kind == PP_SCAN_EXCLUSIVE;
+  r.op = op;
+  r.in = d_in;
+  r.out = d_out;
+  r.n = n;
+  r.offsets = d_offsets;
+  r.num_segments = num_segments;
+  return to_c(seg_dispatch(r, dtype, 0));
+}
+
+pp_status pp_segmented_reduce(pp_stream stream, pp_op op, pp_dtype dtype, const void* d_in, uint64_t n,
+                              const int64_t* d_offsets, uint64_t num_segments, void* d_out) {
+  if (!valid_op(op) || !valid_dtype(dtype)) return PP_ERR_INVALID_ARG;
+  if (!valid_seg_op(op)) return PP_ERR_UNSUPPORTED;
+  if (num_segments == 0) return PP_OK;
+  if (!d_offsets || !d_out || (n > 0 && !d_in)) return PP_ERR_INVALID_ARG;
+  pp::capi::SegReq r;
+  r.s = static_cast<cudaStream_t>(stream);
+  r.op = op;
+  r.in = d_in;
+  r.out = d_out;
+  r.n = n;
+  r.offsets = d_offsets;
+  r.num_segments = num_segments;
+  return to_c(seg_dispatch(r, dtype, 1));
+}
+
+pp_status pp_rows_scan(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dtype, const void* d_in, void* d_out,
+                       uint64_t rows, uint64_t cols, int reverse) {
+  if (!valid_kind(kind) || !valid_op(op) || !valid_dtype(dtype)) return PP_ERR_INVALID_ARG;
+  if (!valid_seg_op(op)) return PP_ERR_UNSUPPORTED;
+  if (rows == 0 || cols == 0) return PP_OK;
+  if (!d_in || !d_out) return PP_ERR_INVALID_ARG;
+  pp::capi::SegReq r;
+  r.s = static_cast<cudaStream_t>(stream);
+  r.exclusive = kind == PP_SCAN_EXCLUSIVE;
+  r.op = op;
+  r.in = d_in;
+  r.out = d_out;
+  r.rows = rows;
+  r.cols = cols;
+  r.reverse = reverse != 0;
+  return to_c(seg_dispatch(r, dtype, 2));
+}
+
 const char* pp_version(void) { return "ppgb300 0.1.0 (sm_103a)"; }
 
 }  // extern "C"

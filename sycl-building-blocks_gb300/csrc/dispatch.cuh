@@ -37,6 +37,26 @@ Status reduce_typed(cudaStream_t s, pp_op op, const void* in, uint64_t n, void* 
 template <class T>
 size_t workspace_typed(pp_scan_algo algo, const void* in, const void* out, uint64_t n);
 
+// Batched segmented scan / reduce and row scans (capi_seg_<type>.cu).
+struct SegReq {
+  cudaStream_t s = nullptr;
+  bool exclusive = false;
+  pp_op op = PP_OP_PLUS;
+  const void* in = nullptr;
+  void* out = nullptr;
+  uint64_t n = 0;
+  const int64_t* offsets = nullptr;
+  uint64_t num_segments = 0;
+  uint64_t rows = 0, cols = 0;
+  bool reverse = false;
+};
+template <class T>
+Status seg_scan_typed(const SegReq& r);
+template <class T>
+Status seg_reduce_typed(const SegReq& r);
+template <class T>
+Status rows_scan_typed(const SegReq& r);
+
 // F32 plus-scan with a precision mode (capi_precision.cu).
 Status scan_f32_precision(const ScanReq& r, pp_precision prec);
 size_t workspace_f32_precision(pp_scan_algo algo, pp_precision prec, const void* in, const void* out, uint64_t n);

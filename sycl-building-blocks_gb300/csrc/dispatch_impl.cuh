@@ -86,6 +86,53 @@ size_t workspace_typed(pp_scan_algo algo, const void* in, const void* out, uint6
   return workspace_policy<PlainScan<T, plus>>(algo, in, out, n);
 }
 
+// Segmented operators: plus, minimum, maximum.
+template <class T, class F>
+Status with_seg_op(pp_op op, F&& f) {
+  switch (op) {
+    case PP_OP_PLUS:
+      return f(plus{});
+    case PP_OP_MINIMUM:
+      return f(minimum{});
+    case PP_OP_MAXIMUM:
+      return f(maximum{});
+    default:
+      return Status::unsupported;
+  }
+}
+
+template <class T>
+Status seg_scan_typed(const SegReq& r) {
+  return with_seg_op<T>(r.op, [&](auto op) {
+    using Op = decltype(op);
+    return host::segmented_scan<T, Op>(r.s, static_cast<const T*>(r.in), static_cast<T*>(r.out), r.n, r.offsets,
+                                       r.num_segments, r.exclusive);
+  });
+}
+
+template <class T>
+Status seg_reduce_typed(const SegReq& r) {
+  return with_seg_op<T>(r.op, [&](auto op) {
+    using Op = decltype(op);
+    return host::segmented_reduce<T, Op>(r.s, static_cast<const T*>(r.in), r.n, r.offsets, r.num_segments,
+                                         static_cast<T*>(r.out));
+  });
+}
+
+template <class T>
+Status rows_scan_typed(const SegReq& r) {
+  return with_seg_op<T>(r.op, [&](auto op) {
+    using Op = decltype(op);
+    return host::rows_scan<T, Op>(r.s, static_cast<const T*>(r.in), static_cast<T*>(r.out), r.rows, r.cols,
+                                  r.exclusive, r.reverse);
+  });
+}
+
+#define PP_INSTANTIATE_SEG(T)                     \
+  template Status seg_scan_typed<T>(const SegReq&);   \
+  template Status seg_reduce_typed<T>(const SegReq&); \
+  template Status rows_scan_typed<T>(const SegReq&);
+
 #define PP_INSTANTIATE_DISPATCH(T)                                                                     \
   template Status scan_typed<T>(const ScanReq&);                                                       \
   template Status reduce_typed<T>(cudaStream_t, pp_op, const void*, uint64_t, void*, void*, size_t); \

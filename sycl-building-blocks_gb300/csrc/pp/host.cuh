@@ -22,6 +22,7 @@
 #include "decoupled_scan.cuh"
 #include "reduce.cuh"
 #include "scan_policy.cuh"
+#include "segmented.cuh"
 #include "workspace.cuh"
 
 namespace pp {
@@ -79,11 +80,14 @@ inline Status device_info(DeviceInfo& out) {
 // streams never do.
 class WorkspaceCache {
  public:
-  Status get(cudaStream_t s, size_t need, void** out) {
+  // kind 0: control words + look-back descriptors (only ever holds descriptor
+  // words past the header, so stale contents are always older-epoch
+  // descriptors or zero); kind 1: general scratch (head bitmaps, ranks).
+  Status get(cudaStream_t s, size_t need, void** out, int kind = 0) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return Status::no_device;
     std::lock_guard<std::mutex> g(mu_);
-    Entry& e = map_[{dev, reinterpret_cast<uintptr_t>(s)}];
+    Entry& e = map_[Key{dev, reinterpret_cast<uintptr_t>(s), kind}];
     if (e.bytes >= need) {
       *out = e.ptr;
       return Status::ok;
@@ -104,12 +108,12 @@ class WorkspaceCache {
     *out = p;
     return Status::ok;
   }
-  // Returns the workspace of this stream if one exists.
+  // Returns the control workspace of this stream if one exists.
   void* find(cudaStream_t s) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
     std::lock_guard<std::mutex> g(mu_);
-    auto it = map_.find({dev, reinterpret_cast<uintptr_t>(s)});
+    auto it = map_.find(Key{dev, reinterpret_cast<uintptr_t>(s), 0});
     return it == map_.end() ? nullptr : it->second.ptr;
   }
   static WorkspaceCache& instance() {
@@ -122,8 +126,18 @@ class WorkspaceCache {
     void* ptr = nullptr;
     size_t bytes = 0;
   };
+  struct Key {
+    int dev;
+    uintptr_t stream;
+    int kind;
+    bool operator<(const Key& o) const {
+      if (dev != o.dev) return dev < o.dev;
+      if (stream != o.stream) return stream < o.stream;
+      return kind < o.kind;
+    }
+  };
   std::mutex mu_;
-  std::map<std::pair<int, uintptr_t>, Entry> map_;
+  std::map<Key, Entry> map_;
 };
 
 // A workspace either supplied by the caller (must have been zero-filled once
@@ -383,6 +397,191 @@ inline Status reduce(cudaStream_t s, const T* in, uint64_t n, T* d_result, void*
   a.partials = w.aux;
   k<<<unsigned(grid), Tn::BLOCK, 0, s>>>(a);
   return from_cuda(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
+// Batched segmented scan / reduce and row scans (segmented.cuh).
+// Variant of the segmented kernel: 4-byte elements take the autotuned one
+// (seg_tuned.inc, written by ppautotune.py), others 16 warps x 16-byte chunks.
+#include "seg_tuned.inc"
+template <class T>
+struct SegTuning {
+  static constexpr bool k4 = sizeof(T) == 4;
+  static constexpr int NC = k4 ? PP_SEG_TUNED_4B_NC : 16;
+  static constexpr int VB = k4 ? PP_SEG_TUNED_4B_VB : 16;
+  static constexpr int ITEMS = k4 ? PP_SEG_TUNED_4B_ITEMS : 16;
+  static constexpr int CH = ITEMS / (VB / int(sizeof(T)));
+  static constexpr int TILE_BYTES = NC * 32 * ITEMS * int(sizeof(T));
+  static constexpr int STAGES = (196608 / TILE_BYTES) < 2 ? 2 : ((196608 / TILE_BYTES) > 8 ? 8 : (196608 / TILE_BYTES));
+  static constexpr int LBW = 4;
+};
+
+template <class T, class Op>
+using SegCfgFor = SegCfg<SegPlainScan<T, Op>, SegTuning<T>::NC, SegTuning<T>::CH, SegTuning<T>::STAGES,
+                         SegTuning<T>::LBW, SegTuning<T>::VB>;
+
+// Control workspace: header + descriptors (room for both the segmented pass
+// and the rank scan of a reduce). Scratch workspace (a separate buffer, so
+// descriptor memory never holds anything but descriptor words): head bitmap,
+// nonempty flags, ranks, rank -> segment map.
+struct SegWsLayout {
+  size_t control_bytes;
+  size_t bitmap_off, bitmap_bytes, nonempty_off, rank_off, r2s_off, scratch_bytes;
+};
+template <class T, class Op>
+inline SegWsLayout seg_ws_layout(uint64_t n, uint64_t num_segments, bool csr, bool reduce) {
+  using Cfg = SegCfgFor<T, Op>;
+  SegWsLayout L{};
+  const uint64_t ntiles = (n + Cfg::TILE - 1) / Cfg::TILE;
+  uint64_t words = ntiles * desc_codec<typename SegPlainScan<T, Op>::carry_t>::W;
+  if (reduce) {
+    const uint64_t rt = (num_segments + StagedFor<PlainScan<uint32_t, plus>>::TILE - 1) /
+                        StagedFor<PlainScan<uint32_t, plus>>::TILE;
+    if (rt > words) words = rt;
+  }
+  L.control_bytes = workspace_bytes_for_desc_words(words);
+  size_t off = 0;
+  L.bitmap_off = off;
+  L.bitmap_bytes = csr ? align_up(((n + 127) / 128) * 16 + Cfg::MAP_BYTES, 256) : 0;
+  off += L.bitmap_bytes;
+  L.nonempty_off = off;
+  if (reduce) off += align_up(num_segments * 4, 256);
+  L.rank_off = off;
+  if (reduce) off += align_up(num_segments * 4, 256);
+  L.r2s_off = off;
+  if (reduce) off += align_up(num_segments * 4, 256);
+  L.scratch_bytes = off;
+  return L;
+}
+
+inline Status acquire_scratch(cudaStream_t s, size_t need, unsigned char** out) {
+  void* p = nullptr;
+  Status st = WorkspaceCache::instance().get(s, need ? need : 256, &p, 1);
+  *out = static_cast<unsigned char*>(p);
+  return st;
+}
+
+template <class Pol, class Heads, bool REVERSE, bool REDUCE>
+inline Status launch_segmented(cudaStream_t s, const SegArgs& a) {
+  using Tn = SegTuning<typename Pol::in_t>;
+  using Cfg = SegCfg<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Tn::VB>;
+  auto k = segmented_staged_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Heads, REVERSE, REDUCE, Tn::VB>;
+  DeviceInfo di;
+  Status st = device_info(di);
+  if (st != Status::ok) return st;
+  int bps = 0;
+  st = prepare_kernel(k, Cfg::THREADS, Cfg::SMEM, bps);
+  if (st != Status::ok) return st;
+  const uint64_t ntiles = (a.s.n + Cfg::TILE - 1) / Cfg::TILE;
+  uint64_t grid = uint64_t(bps) * di.sm_count;
+  const int cap = settings().max_ctas.load();
+  if (cap > 0 && uint64_t(cap) < grid) grid = cap;
+  if (ntiles < grid) grid = ntiles;
+  k<<<unsigned(grid), Cfg::THREADS, Cfg::SMEM, s>>>(a);
+  return from_cuda(cudaGetLastError());
+}
+
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// CSR segmented scan: offsets[0] = 0, offsets[num_segments] = n, nondecreasing.
+template <class T, class Op>
+inline Status segmented_scan(cudaStream_t s, const T* in, T* out, uint64_t n, const int64_t* offsets,
+                             uint64_t num_segments, bool exclusive, void* user_ws = nullptr,
+                             size_t user_ws_bytes = 0) {
+  if (n == 0 || num_segments == 0) return Status::ok;
+  if (!in || !out || !offsets) return Status::invalid_arg;
+  if (!aligned16(in) || !aligned16(out)) return Status::invalid_arg;
+  const SegWsLayout L = seg_ws_layout<T, Op>(n, num_segments, true, false);
+  Ws w;
+  Status st = acquire_ws(s, L.control_bytes, user_ws, user_ws_bytes, w);
+  if (st != Status::ok) return st;
+  unsigned char* base = nullptr;
+  st = acquire_scratch(s, L.scratch_bytes, &base);
+  if (st != Status::ok) return st;
+  uint32_t* heads = reinterpret_cast<uint32_t*>(base + L.bitmap_off);
+  if (cudaMemsetAsync(heads, 0, L.bitmap_bytes, s) != cudaSuccess) return Status::cuda;
+  const unsigned pre_grid = unsigned((num_segments + 255) / 256 < 1024 ? (num_segments + 255) / 256 : 1024);
+  segment_heads_kernel<T, Op><<<pre_grid, 256, 0, s>>>(offsets, num_segments, n, heads, nullptr, nullptr);
+  if (cudaGetLastError() != cudaSuccess) return Status::cuda;
+  SegArgs a{};
+  a.s.in = in;
+  a.s.out = out;
+  a.s.n = n;
+  a.s.hdr = w.hdr;
+  a.s.desc = w.desc;
+  a.s.timeout_ns = settings().timeout_ns.load();
+  a.s.debug_skip_tile = -1;
+  a.s.exclusive = exclusive ? 1 : 0;
+  a.heads = heads;
+  return launch_segmented<SegPlainScan<T, Op>, CsrHeads, false, false>(s, a);
+}
+
+// CSR segmented reduce: out[s] = op-reduction of segment s (identity if empty).
+template <class T, class Op>
+inline Status segmented_reduce(cudaStream_t s, const T* in, uint64_t n, const int64_t* offsets,
+                               uint64_t num_segments, T* out, void* user_ws = nullptr, size_t user_ws_bytes = 0) {
+  if (num_segments == 0) return Status::ok;
+  if (!offsets || !out || (n > 0 && !in)) return Status::invalid_arg;
+  if (n > 0 && !aligned16(in)) return Status::invalid_arg;
+  const SegWsLayout L = seg_ws_layout<T, Op>(n, num_segments, true, true);
+  Ws w;
+  Status st = acquire_ws(s, L.control_bytes, user_ws, user_ws_bytes, w);
+  if (st != Status::ok) return st;
+  unsigned char* base = nullptr;
+  st = acquire_scratch(s, L.scratch_bytes, &base);
+  if (st != Status::ok) return st;
+  uint32_t* heads = reinterpret_cast<uint32_t*>(base + L.bitmap_off);
+  uint32_t* nonempty = reinterpret_cast<uint32_t*>(base + L.nonempty_off);
+  uint32_t* rank = reinterpret_cast<uint32_t*>(base + L.rank_off);
+  uint32_t* r2s = reinterpret_cast<uint32_t*>(base + L.r2s_off);
+  if (cudaMemsetAsync(heads, 0, L.bitmap_bytes, s) != cudaSuccess) return Status::cuda;
+  const unsigned pre_grid = unsigned((num_segments + 255) / 256 < 1024 ? (num_segments + 255) / 256 : 1024);
+  segment_heads_kernel<T, Op><<<pre_grid, 256, 0, s>>>(offsets, num_segments, n, heads, nonempty, out);
+  if (cudaGetLastError() != cudaSuccess) return Status::cuda;
+  if (n == 0) return Status::ok;
+  st = decoupled_scan<PlainScan<uint32_t, plus>>(s, nonempty, rank, num_segments, true, w.hdr, L.control_bytes);
+  if (st != Status::ok) return st;
+  segment_rank_kernel<<<pre_grid, 256, 0, s>>>(nonempty, rank, num_segments, r2s);
+  if (cudaGetLastError() != cudaSuccess) return Status::cuda;
+  SegArgs a{};
+  a.s.in = in;
+  a.s.out = nullptr;
+  a.s.n = n;
+  a.s.hdr = w.hdr;
+  a.s.desc = w.desc;
+  a.s.timeout_ns = settings().timeout_ns.load();
+  a.s.debug_skip_tile = -1;
+  a.heads = heads;
+  a.rank_to_seg = r2s;
+  a.seg_out = out;
+  return launch_segmented<SegPlainScan<T, Op>, CsrHeads, false, true>(s, a);
+}
+
+// Row scans of a rows x cols row-major matrix (every row its own segment);
+// reverse = suffix scans.
+template <class T, class Op>
+inline Status rows_scan(cudaStream_t s, const T* in, T* out, uint64_t rows, uint64_t cols, bool exclusive,
+                        bool reverse, void* user_ws = nullptr, size_t user_ws_bytes = 0) {
+  const uint64_t n = rows * cols;
+  if (n == 0) return Status::ok;
+  if (!in || !out) return Status::invalid_arg;
+  if (!aligned16(in) || !aligned16(out)) return Status::invalid_arg;
+  const SegWsLayout L = seg_ws_layout<T, Op>(n, 0, false, false);
+  Ws w;
+  Status st = acquire_ws(s, L.control_bytes, user_ws, user_ws_bytes, w);
+  if (st != Status::ok) return st;
+  SegArgs a{};
+  a.s.in = in;
+  a.s.out = out;
+  a.s.n = n;
+  a.s.hdr = w.hdr;
+  a.s.desc = w.desc;
+  a.s.timeout_ns = settings().timeout_ns.load();
+  a.s.debug_skip_tile = -1;
+  a.s.exclusive = exclusive ? 1 : 0;
+  a.seg_len = cols;
+  if (reverse) return launch_segmented<SegPlainScan<T, Op>, UniformHeads, true, false>(s, a);
+  return launch_segmented<SegPlainScan<T, Op>, UniformHeads, false, false>(s, a);
 }
 
 }  // namespace host

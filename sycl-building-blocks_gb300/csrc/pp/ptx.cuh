@@ -65,6 +65,24 @@ __device__ __forceinline__ void st_stream_v4(void* p, uint4 v) {
                "r"(v.w)
                : "memory");
 }
+__device__ __forceinline__ void st_stream_v2(void* p, uint2 v) {
+  asm volatile("st.global.cs.v2.u32 [%0], {%1, %2};" ::"l"(p), "r"(v.x), "r"(v.y) : "memory");
+}
+__device__ __forceinline__ void st_stream_u32(void* p, uint32_t v) {
+  asm volatile("st.global.cs.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// Streaming store of 4, 8 or 16 bytes.
+template <int BYTES>
+__device__ __forceinline__ void st_stream(void* p, const void* src) {
+  if constexpr (BYTES == 16) {
+    st_stream_v4(p, *static_cast<const uint4*>(src));
+  } else if constexpr (BYTES == 8) {
+    st_stream_v2(p, *static_cast<const uint2*>(src));
+  } else {
+    static_assert(BYTES == 4, "4, 8 or 16 bytes");
+    st_stream_u32(p, *static_cast<const uint32_t*>(src));
+  }
+}
 __device__ __forceinline__ uint4 ld_stream_v4(const void* p) {
   uint4 v;
   asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"

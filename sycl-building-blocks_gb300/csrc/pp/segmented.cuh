@@ -1,0 +1,495 @@
+// Batched segmented scan / reduce for sm_103a: many independent segments of
+// uneven length, laid out back to back (CSR: int64 offsets, S + 1 entries,
+// offsets[0] = 0, offsets[S] = n), in ONE persistent launch of the staged
+// decoupled look-back pipeline (decoupled_scan.cuh) instead of one launch per
+// segment. No counterpart in the reference, which scans one array per call.
+//
+// Segments become a segmented operator on (value, count) pairs:
+//     (a, c) op (b, d) = (d ? b : a op b, c + d)
+// where d counts the segment heads inside the right operand. It is
+// associative, so tiles may cross segment boundaries freely and the look-back
+// stops contributing at the nearest head. The count also ranks every element:
+// the inclusive count at element e is the number of distinct segment starts
+// at or before e.
+//
+// Head flags come from a bitmap of n bits (one per element): a pre-pass
+// scatters the start of every non-empty segment into it, and the producer warp
+// bulk-copies each tile's 2 KB slice of the bitmap into shared memory next to
+// the tile's data. Uniform segments (rows of equal length, as for a batched
+// cumsum) need no bitmap: heads are computed from the index.
+//
+// Reverse scans (suffix sums, the adjoint of a prefix sum) walk the tiles from
+// the last to the first and mirror the element order inside each tile; they
+// are provided for uniform segments.
+//
+// Segmented reduce reuses the same pass without writing the scanned array:
+// the element that ends a non-empty segment writes the segment's value to
+// out[rank_to_segment[count - 1]]; empty segments get the identity from the
+// pre-pass.
+#pragma once
+
+#include <cstdint>
+#include <type_traits>
+#include <cuda_runtime.h>
+
+#include "decoupled_scan.cuh"
+
+namespace pp {
+
+template <class T>
+struct seg_pair {
+  T v;
+  uint32_t c;  // segment heads covered by this partial
+};
+
+// Segmented plain policy over (value, head-count) pairs.
+template <class T, class Op>
+struct SegPlainScan {
+  using in_t = T;
+  using out_t = T;
+  using acc_t = seg_pair<T>;
+  using carry_t = seg_pair<T>;
+  using pre_t = seg_pair<T>;
+  Op op;
+
+  __device__ __forceinline__ acc_t aop(const acc_t& a, const acc_t& b) const {
+    return acc_t{b.c ? b.v : op(a.v, b.v), a.c + b.c};
+  }
+  __device__ __forceinline__ acc_t aid() const { return acc_t{identity<Op, T>(), 0u}; }
+  __device__ __forceinline__ carry_t cop(const carry_t& a, const carry_t& b) const { return aop(a, b); }
+  __device__ __forceinline__ carry_t cid() const { return aid(); }
+  __device__ __forceinline__ carry_t to_carry(const acc_t& a) const { return a; }
+  __device__ __forceinline__ acc_t load(const T& x, bool head) const { return acc_t{x, head ? 1u : 0u}; }
+};
+
+// Where segment heads are.
+struct CsrHeads {
+  static constexpr bool kBitmap = true;
+  uint64_t len = 0;  // unused
+};
+struct UniformHeads {
+  static constexpr bool kBitmap = false;
+  uint64_t len = 1;  // segment (row) length
+};
+
+struct SegArgs {
+  ScanArgs s;
+  const uint32_t* heads;         // CSR: n-bit head bitmap (tile-padded), else null
+  uint64_t seg_len;              // uniform: row length
+  const uint32_t* rank_to_seg;   // reduce: non-empty segment rank -> segment id
+  void* seg_out;                 // reduce: per-segment output
+};
+
+// NC compute warps, CH chunks per lane, VB bytes per chunk (the vector width
+// of shared-memory loads and global stores: 4, 8 or 16), STAGES-deep ring.
+template <class Pol, int NC_, int CH_, int STAGES_, int LBW_, int VB_ = 16>
+struct SegCfg {
+  using in_t = typename Pol::in_t;
+  using acc_t = typename Pol::acc_t;
+  using carry_t = typename Pol::carry_t;
+  static constexpr int NC = NC_;
+  static constexpr int CH = CH_;
+  static constexpr int STAGES = STAGES_;
+  static constexpr int LBW = LBW_;
+  static constexpr int VB = VB_;
+  static_assert(VB == 4 || VB == 8 || VB == 16, "chunk width of 4, 8 or 16 bytes");
+  static_assert(VB % sizeof(in_t) == 0, "element size must divide the chunk width");
+  static constexpr int V = VB / int(sizeof(in_t));
+  static constexpr int SEG = 32 * CH * V;
+  static constexpr int TILE = NC * SEG;
+  static_assert(TILE % 128 == 0, "tile must cover whole 16-byte bitmap words");
+  static constexpr int TILE_BYTES = TILE * int(sizeof(in_t));
+  static constexpr int MAP_BYTES = TILE / 8;  // head bits of one tile
+  static constexpr int THREADS = (NC + 2) * 32;
+  static constexpr size_t META_AGG = 0;
+  static constexpr size_t META_PREF = align_up(NC * sizeof(acc_t), 16);
+  static constexpr size_t META_TAGG = META_PREF + align_up(sizeof(carry_t), 16);
+  static constexpr size_t META_TILE = META_TAGG + align_up(sizeof(carry_t), 8);
+  static constexpr size_t META_CNT = META_TILE + 8;
+  static constexpr size_t META_BYTES = align_up(META_CNT + 4, 16);
+  static constexpr size_t OFF_MAP = size_t(STAGES) * TILE_BYTES;
+  static constexpr size_t OFF_META = OFF_MAP + size_t(STAGES) * MAP_BYTES;
+  static constexpr size_t OFF_BAR = align_up(OFF_META + STAGES * META_BYTES, 8);
+  static constexpr size_t SMEM = OFF_BAR + 4 * STAGES * 8;
+};
+
+// REDUCE: write only segment totals (via rank_to_seg) instead of the scan.
+template <class Pol, int NC, int CH, int STAGES, int LBW, class Heads, bool REVERSE, bool REDUCE, int VB = 16>
+__global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(const SegArgs sargs) {
+  using Cfg = SegCfg<Pol, NC, CH, STAGES, LBW, VB>;
+  using vec_t = std::conditional_t<VB == 16, uint4, std::conditional_t<VB == 8, uint2, uint32_t>>;
+  using in_t = typename Pol::in_t;
+  using out_t = typename Pol::out_t;
+  using acc_t = typename Pol::acc_t;
+  using carry_t = typename Pol::carry_t;
+  using codec = desc_codec<carry_t>;
+  constexpr int V = Cfg::V;
+  constexpr int TILE = Cfg::TILE;
+  static_assert(!(REVERSE && Heads::kBitmap), "reverse scans are provided for uniform segments");
+  static_assert(!(REVERSE && REDUCE), "reverse segmented reduce is not provided");
+
+  const ScanArgs& args = sargs.s;
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + Cfg::OFF_BAR);
+  uint64_t* full = bars;
+  uint64_t* empty = bars + STAGES;
+  uint64_t* aggb = bars + 2 * STAGES;
+  uint64_t* prefb = bars + 3 * STAGES;
+  auto meta = [&](int s) { return smem + Cfg::OFF_META + size_t(s) * Cfg::META_BYTES; };
+  auto s_aggs = [&](int s) { return reinterpret_cast<acc_t*>(meta(s) + Cfg::META_AGG); };
+  auto s_pref = [&](int s) { return reinterpret_cast<carry_t*>(meta(s) + Cfg::META_PREF); };
+  auto s_tagg = [&](int s) { return reinterpret_cast<carry_t*>(meta(s) + Cfg::META_TAGG); };
+  auto s_tile = [&](int s) { return reinterpret_cast<long long*>(meta(s) + Cfg::META_TILE); };
+  auto s_cnt = [&](int s) { return reinterpret_cast<unsigned*>(meta(s) + Cfg::META_CNT); };
+  auto s_map = [&](int s) { return reinterpret_cast<const uint32_t*>(smem + Cfg::OFF_MAP + size_t(s) * Cfg::MAP_BYTES); };
+
+  const Pol pol{};
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const uint64_t n = args.n;
+  const long long ntiles = (long long)((n + TILE - 1) / TILE);
+  WsHeader* hdr = args.hdr;
+  const uint64_t tmo = args.timeout_ns;
+  // ticket k (sequence position) -> physical tile
+  auto phys = [&](long long k) { return REVERSE ? ntiles - 1 - k : k; };
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      ptx::mbar_init(&full[s], 1);
+      ptx::mbar_init(&empty[s], NC);
+      ptx::mbar_init(&aggb[s], NC);
+      ptx::mbar_init(&prefb[s], 1);
+      *s_cnt(s) = 0u;
+    }
+    ptx::fence_mbar_init();
+  }
+  __syncthreads();
+  const uint32_t etag = ptx::ld_relaxed(reinterpret_cast<const uint32_t*>(&hdr->epoch)) + 1u;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      const uint64_t pol_l2 = ptx::policy_evict_first();
+      const unsigned char* in = static_cast<const unsigned char*>(args.in);
+      uint32_t pending = 0, pend_par = 0;
+      long long t = (long long)atomicAdd(&hdr->ticket, 1ull);
+      for (int k = 0;; ++k) {
+        const int s = k % STAGES;
+        if (k >= STAGES) {
+          if (!mbar_wait_bounded(&empty[s], ((k / STAGES) - 1) & 1, hdr, tmo, (unsigned long long)t)) break;
+          pending &= ~(1u << s);
+        }
+        *s_tile(s) = t;
+        if (t < ntiles) {
+          const uint64_t base = uint64_t(phys(t)) * TILE;
+          const uint64_t valid = (n - base < uint64_t(TILE)) ? (n - base) : uint64_t(TILE);
+          const uint32_t bytes = uint32_t(valid * sizeof(in_t)) & ~15u;
+          uint32_t map_bytes = 0;
+          if constexpr (Heads::kBitmap) map_bytes = uint32_t((valid + 127) / 128) * 16u;
+          if (bytes + map_bytes) {
+            ptx::mbar_arrive_expect_tx(&full[s], bytes + map_bytes);
+            if (bytes)
+              ptx::bulk_g2s(smem + size_t(s) * Cfg::TILE_BYTES, in + base * sizeof(in_t), bytes, &full[s], pol_l2);
+            if (map_bytes)
+              ptx::bulk_g2s(smem + Cfg::OFF_MAP + size_t(s) * Cfg::MAP_BYTES,
+                            reinterpret_cast<const unsigned char*>(sargs.heads) + base / 8, map_bytes, &full[s],
+                            pol_l2);
+            pending |= 1u << s;
+            pend_par = (pend_par & ~(1u << s)) | ((uint32_t(k / STAGES) & 1u) << s);
+          } else {
+            ptx::mbar_arrive(&full[s]);
+          }
+          t = (long long)atomicAdd(&hdr->ticket, 1ull);
+        } else {
+          ptx::mbar_arrive(&full[s]);
+          break;
+        }
+      }
+      for (int s = 0; s < STAGES; ++s)
+        if (pending & (1u << s)) mbar_wait_bounded(&full[s], (pend_par >> s) & 1u, hdr, tmo, 0ull);
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ look-back
+    for (int k = 0;; ++k) {
+      const int s = k % STAGES;
+      const uint32_t par = (k / STAGES) & 1;
+      if (!mbar_wait_bounded(&full[s], par, hdr, tmo, 0ull)) break;
+      const long long tile = *s_tile(s);
+      if (tile >= ntiles) break;
+      uint32_t peek_st = kInvalid;
+      carry_t peek_v = pol.cid();
+      if (lane == 0 && tile > 0) peek_st = codec::read(args.desc + (tile - 1) * codec::W, etag, peek_v);
+      if (!mbar_wait_bounded(&aggb[s], par, hdr, tmo, 0ull)) break;
+      const carry_t agg = *s_tagg(s);
+      uint64_t* d = args.desc + tile * codec::W;
+      carry_t excl = pol.cid();
+      bool ok = true;
+      unsigned long long stats = 0;
+      if (tile == 0) {
+      } else if (__shfl_sync(kFullMask, peek_st, 0) == kPrefix) {
+        excl = shfl_idx(peek_v, 0);
+        if (lane == 0) codec::publish(d, pol.cop(excl, agg), make_tag(etag, kPrefix));
+      } else {
+        ok = lookback_multi<Pol, LBW>(pol, args.desc, tile, etag, hdr, tmo, lane, excl, stats);
+        if (ok && lane == 0) codec::publish(d, pol.cop(excl, agg), make_tag(etag, kPrefix));
+      }
+      if (!ok) break;
+      if (lane == 0) {
+        *s_pref(s) = excl;
+        ptx::mbar_arrive(&prefb[s]);
+      }
+      __syncwarp();
+    }
+  } else {
+    // ------------------------------------------------------------ compute
+    const int w = warp - 2;
+    const in_t* gin = static_cast<const in_t*>(args.in);
+    out_t* gout = static_cast<out_t*>(args.out);
+    const bool excl_kind = args.exclusive != 0;
+    auto aop = [&](const acc_t& x, const acc_t& y) { return pol.aop(x, y); };
+    const uint64_t seg_len = sargs.seg_len;
+
+    // Loads logical chunk c of this lane (V consecutive sequence positions).
+    // Returns the head bits of the V elements (bit j for element j).
+    auto load_chunk = [&](int s, int c, uint64_t base, int valid, int bulk, in_t (&x)[V]) -> uint32_t {
+      const unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
+      const int e0 = w * Cfg::SEG + (c * 32 + lane) * V;  // logical tile offset
+      uint32_t hb = 0;
+      if (!REVERSE || valid == TILE) {
+        // physical positions p_j = e0 + j (forward) or TILE - 1 - (e0 + j) (reverse)
+        const int p0 = REVERSE ? TILE - V - e0 : e0;
+        if (p0 + V <= bulk) {
+          union {
+            vec_t u;
+            in_t v[V];
+          } buf;
+          buf.u = *reinterpret_cast<const vec_t*>(stage + size_t(p0) * sizeof(in_t));
+#pragma unroll
+          for (int j = 0; j < V; ++j) x[j] = buf.v[REVERSE ? V - 1 - j : j];
+        } else {
+#pragma unroll
+          for (int j = 0; j < V; ++j) {
+            const int p = REVERSE ? TILE - 1 - (e0 + j) : e0 + j;
+            if (p < bulk)
+              x[j] = reinterpret_cast<const in_t*>(stage)[p];
+            else if (p < valid)
+              x[j] = gin[base + p];
+            else
+              x[j] = identity<decltype(pol.op), in_t>();
+          }
+        }
+      } else {
+        // partial tile of a reverse scan: logical e -> physical valid - 1 - e
+#pragma unroll
+        for (int j = 0; j < V; ++j) {
+          const int e = e0 + j;
+          const int p = valid - 1 - e;
+          if (e < valid)
+            x[j] = p < bulk ? reinterpret_cast<const in_t*>(stage)[p] : gin[base + p];
+          else
+            x[j] = identity<decltype(pol.op), in_t>();
+        }
+      }
+      if constexpr (Heads::kBitmap) {
+        const uint32_t word = s_map(s)[e0 >> 5];
+        hb = (word >> (e0 & 31)) & ((1u << V) - 1u);
+        if (e0 + V > valid) hb &= (e0 >= valid) ? 0u : ((1u << (valid - e0)) - 1u);
+      } else {
+#pragma unroll
+        for (int j = 0; j < V; ++j) {
+          const int e = e0 + j;
+          if (e < valid) {
+            // global physical index of sequence position e
+            const uint64_t g = REVERSE ? (valid == TILE ? base + uint64_t(TILE - 1 - e) : base + uint64_t(valid - 1 - e))
+                                       : base + uint64_t(e);
+            // forward: a row starts at g % len == 0; reverse: at the row's last element
+            const bool h = REVERSE ? ((g + 1) % seg_len == 0) : (g % seg_len == 0);
+            hb |= uint32_t(h) << j;
+          }
+        }
+      }
+      return hb;
+    };
+    auto tile_geom = [&](int s, long long& tile, uint64_t& base, int& valid, int& bulk) {
+      tile = *s_tile(s);
+      base = uint64_t(phys(tile)) * TILE;
+      const uint64_t rem = n - base;
+      valid = rem < uint64_t(TILE) ? int(rem) : TILE;
+      bulk = int((uint32_t(valid * sizeof(in_t)) & ~15u) / sizeof(in_t));
+    };
+    auto reduce_pass = [&](int k) -> bool {
+      const int s = k % STAGES;
+      if (!mbar_wait_bounded(&full[s], (k / STAGES) & 1, hdr, tmo, 0ull)) return false;
+      long long tile;
+      uint64_t base;
+      int valid, bulk;
+      tile_geom(s, tile, base, valid, bulk);
+      if (tile >= ntiles) return false;
+      acc_t r = pol.aid();
+      for (int c = 0; c < CH; ++c) {
+        in_t x[V];
+        const uint32_t hb = load_chunk(s, c, base, valid, bulk, x);
+        acc_t t = pol.load(x[0], hb & 1u);
+#pragma unroll
+        for (int j = 1; j < V; ++j) t = pol.aop(t, pol.load(x[j], (hb >> j) & 1u));
+        r = pol.aop(r, warp_reduce(t, aop, lane));
+      }
+      unsigned last = 0;
+      if (lane == 0) {
+        s_aggs(s)[w] = r;
+        __threadfence_block();
+        last = atomicAdd(s_cnt(s), 1u) == unsigned(NC - 1);
+      }
+      if (__shfl_sync(kFullMask, last, 0)) {
+        __threadfence_block();
+        acc_t x = lane < NC ? s_aggs(s)[lane] : pol.aid();
+        x = warp_inclusive_scan(x, aop, lane);
+        const carry_t agg = pol.to_carry(shfl_idx(x, NC - 1));
+        if (lane == 0) {
+          *s_tagg(s) = agg;
+          *s_cnt(s) = 0u;
+          codec::publish(args.desc + tile * codec::W, agg, make_tag(etag, tile == 0 ? kPrefix : kAggregate));
+        }
+      }
+      __syncwarp();
+      if (lane == 0) ptx::mbar_arrive(&aggb[s]);
+      __syncwarp();
+      return true;
+    };
+
+    bool have = reduce_pass(0);
+    for (int k = 0; have; ++k) {
+      const bool have_next = reduce_pass(k + 1);
+      const int s = k % STAGES;
+      if (!mbar_wait_bounded(&prefb[s], (k / STAGES) & 1, hdr, tmo, 0ull)) break;
+      long long tile;
+      uint64_t base;
+      int valid, bulk;
+      tile_geom(s, tile, base, valid, bulk);
+      acc_t sx = (lane < w) ? s_aggs(s)[lane] : pol.aid();
+      sx = warp_reduce(sx, aop, lane);
+      const acc_t pw = w == 0 ? *s_pref(s) : pol.aop(*s_pref(s), sx);
+      acc_t X = pol.aid();
+      for (int c = 0; c < CH; ++c) {
+        in_t x[V];
+        const uint32_t hb = load_chunk(s, c, base, valid, bulk, x);
+        acc_t a[V];
+        a[0] = pol.load(x[0], hb & 1u);
+#pragma unroll
+        for (int j = 1; j < V; ++j) a[j] = pol.aop(a[j - 1], pol.load(x[j], (hb >> j) & 1u));
+        const acc_t inc = warp_inclusive_scan(a[V - 1], aop, lane);
+        acc_t ex = shfl_up(inc, 1);
+        if (lane == 0) ex = pol.aid();
+        const acc_t pc = pol.aop(pw, c == 0 ? ex : pol.aop(X, ex));  // everything before this chunk
+        X = (c == 0) ? shfl_idx(inc, 31) : pol.aop(X, shfl_idx(inc, 31));
+        const int e0 = w * Cfg::SEG + (c * 32 + lane) * V;
+        if constexpr (!REDUCE) {
+          union {
+            vec_t u;
+            out_t v[V];
+          } o;
+#pragma unroll
+          for (int j = 0; j < V; ++j) {
+            if (excl_kind) {
+              // exclusive: identity at a head, else the inclusive value before
+              const acc_t before = j == 0 ? pc : pol.aop(pc, a[j - 1]);
+              o.v[j] = ((hb >> j) & 1u) ? pol.aid().v : before.v;
+            } else {
+              o.v[j] = pol.aop(pc, a[j]).v;
+            }
+          }
+          if (!REVERSE || valid == TILE) {
+            const int p0 = REVERSE ? TILE - V - e0 : e0;
+            if (p0 + V <= valid) {
+              if constexpr (REVERSE) {
+                union {
+                  vec_t u;
+                  out_t v[V];
+                } r;
+#pragma unroll
+                for (int j = 0; j < V; ++j) r.v[j] = o.v[V - 1 - j];
+                ptx::st_stream<VB>(gout + base + p0, &r.u);
+              } else {
+                ptx::st_stream<VB>(gout + base + p0, &o.u);
+              }
+            } else {
+#pragma unroll
+              for (int j = 0; j < V; ++j) {
+                const int p = REVERSE ? TILE - 1 - (e0 + j) : e0 + j;
+                if (p < valid) gout[base + p] = o.v[j];
+              }
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < V; ++j)
+              if (e0 + j < valid) gout[base + (valid - 1 - (e0 + j))] = o.v[j];
+          }
+        } else {
+          // segment totals: element e ends a non-empty segment when e + 1 is a
+          // head or e is the last element
+#pragma unroll
+          for (int j = 0; j < V; ++j) {
+            const int e = e0 + j;
+            if (e >= valid) break;
+            bool end;
+            const int e1 = e + 1;
+            if (base + uint64_t(e1) >= n) {
+              end = true;  // the last element of the array ends its segment
+            } else if (j + 1 < V) {
+              end = (hb >> (j + 1)) & 1u;
+            } else if (e1 < valid) {
+              end = (s_map(s)[e1 >> 5] >> (e1 & 31)) & 1u;
+            } else {
+              end = (__ldg(sargs.heads + ((base + uint64_t(e1)) >> 5)) >> ((base + e1) & 31)) & 1u;
+            }
+            if (end) {
+              const acc_t v = pol.aop(pc, a[j]);
+              if (v.c > 0) {
+                const uint32_t seg = __ldg(sargs.rank_to_seg + (v.c - 1));
+                static_cast<out_t*>(sargs.seg_out)[seg] = v.v;
+              }
+            }
+          }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) ptx::mbar_arrive(&empty[s]);
+      have = have_next;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) cta_exit_rearm(hdr, args.desc, uint64_t(ntiles) * codec::W);
+}
+
+// ---------------------------------------------------------------------------
+// Pre-pass for CSR segments: head bitmap, empty segments, ranks.
+//   heads: bit offsets[s] set for every non-empty segment s (bitmap cleared
+//          by the caller);
+//   nonempty[s] = 1 for a non-empty segment (input of the rank scan);
+//   reduce only: out[s] = identity for every empty segment.
+template <class T, class Op>
+__global__ void segment_heads_kernel(const int64_t* offsets, uint64_t num_segments, uint64_t n, uint32_t* heads,
+                                     uint32_t* nonempty, T* reduce_out) {
+  for (uint64_t s = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; s < num_segments;
+       s += uint64_t(gridDim.x) * blockDim.x) {
+    int64_t b = offsets[s], e = offsets[s + 1];
+    if (b < 0) b = 0;
+    if (e > int64_t(n)) e = int64_t(n);
+    const bool ne = e > b;
+    if (nonempty) nonempty[s] = ne ? 1u : 0u;
+    if (ne) atomicOr(heads + (uint64_t(b) >> 5), 1u << (uint64_t(b) & 31));
+    if (reduce_out && !ne) reduce_out[s] = identity<Op, T>();
+  }
+}
+
+// rank_to_seg[rank[s]] = s for every non-empty segment (rank = exclusive scan
+// of nonempty).
+template <class I>
+__global__ void segment_rank_kernel(const I* nonempty, const I* rank, uint64_t num_segments, I* rank_to_seg) {
+  for (uint64_t s = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; s < num_segments;
+       s += uint64_t(gridDim.x) * blockDim.x)
+    if (nonempty[s]) rank_to_seg[rank[s]] = I(s);
+}
+
+}  // namespace pp

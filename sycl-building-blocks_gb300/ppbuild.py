@@ -40,7 +40,8 @@ def _sources() -> list[Path]:
 
 def _hash_inputs(extra: list[str]) -> str:
     h = hashlib.sha256()
-    files = sorted(list(CSRC.rglob("*.cu")) + list(CSRC.rglob("*.cuh")) + list((ROOT / "include").rglob("*.h")))
+    files = sorted(list(CSRC.rglob("*.cu")) + list(CSRC.rglob("*.cuh")) + list(CSRC.rglob("*.inc")) +
+                   list((ROOT / "include").rglob("*.h")))
     for f in files:
         h.update(str(f.relative_to(ROOT)).encode())
         h.update(f.read_bytes())

@@ -47,7 +47,7 @@ EXPORTS = [
     "pp_scan_device", "pp_group_scan_device", "pp_reduce_device", "pp_reduce", "pp_reduce_ws",
     "pp_decoupled_scan_host", "pp_cooperative_scan_host", "pp_scan_host", "pp_reduce_host", "pp_status_string",
     "pp_stream_status", "pp_workspace_status", "pp_set_timeout_ns", "pp_set_max_ctas", "pp_debug_set_skip_tile",
-    "pp_version",
+    "pp_version", "pp_segmented_scan", "pp_segmented_reduce", "pp_rows_scan",
 ]
 
 
@@ -81,6 +81,9 @@ def lib() -> C.CDLL:
     for name in ("pp_decoupled_scan_host", "pp_cooperative_scan_host", "pp_scan_host"):
         getattr(L, name).argtypes = [i32, i32, i32, vp, vp, u64]
     L.pp_reduce_host.argtypes = [i32, i32, vp, u64, vp]
+    L.pp_segmented_scan.argtypes = [vp, i32, i32, i32, vp, vp, u64, vp, u64]
+    L.pp_segmented_reduce.argtypes = [vp, i32, i32, vp, u64, vp, u64, vp]
+    L.pp_rows_scan.argtypes = [vp, i32, i32, i32, vp, vp, u64, u64, i32]
     L.pp_status_string.argtypes = [i32]
     L.pp_status_string.restype = C.c_char_p
     L.pp_stream_status.argtypes = [vp]
@@ -187,6 +190,25 @@ def reduce(op, d_in: int, n: int, dtype, d_result: int, stream: int = 0,
     else:
         st = lib().pp_reduce_ws(stream, _op(op), _dt(dtype), d_in, n, d_result, workspace[0], workspace[1])
     _check(st, "pp_reduce")
+
+
+def segmented_scan(kind, op, d_in: int, d_out: int, n: int, d_offsets: int, num_segments: int, dtype,
+                   stream: int = 0) -> None:
+    """Scan every CSR segment [offsets[s], offsets[s+1]) of d_in independently."""
+    _check(lib().pp_segmented_scan(stream, _kind(kind), _op(op), _dt(dtype), d_in, d_out, n, d_offsets,
+                                   num_segments), "pp_segmented_scan")
+
+
+def segmented_reduce(op, d_in: int, n: int, d_offsets: int, num_segments: int, d_out: int, dtype,
+                     stream: int = 0) -> None:
+    _check(lib().pp_segmented_reduce(stream, _op(op), _dt(dtype), d_in, n, d_offsets, num_segments, d_out),
+           "pp_segmented_reduce")
+
+
+def rows_scan(kind, op, d_in: int, d_out: int, rows: int, cols: int, dtype, reverse: bool = False,
+              stream: int = 0) -> None:
+    _check(lib().pp_rows_scan(stream, _kind(kind), _op(op), _dt(dtype), d_in, d_out, rows, cols, int(reverse)),
+           "pp_rows_scan")
 
 
 # ---- host-array wrappers (blocking) --------------------------------------------
