@@ -174,6 +174,22 @@ pp_status pp_debug_set_skip_tile(long long tile);
 /* Library version string. */
 const char* pp_version(void);
 
+/* ---- allocation-free variant ------------------------------------------------
+ * No counterpart in the reference. The same decoupled look-back scan as
+ * pp_decoupled_scan_device, for callers that cannot allocate device memory
+ * when they scan (inside CUDA-graph capture, in loops that must stay out of
+ * the allocator, in plug-ins whose host framework owns all device memory).
+ * Its scratch is a fixed 1 MiB array in the library's device image instead
+ * of a cudaMalloc'd or per-stream cached workspace, so it allocates nothing.
+ * Limit: n up to 1,870,659,584 elements of a 4-byte type or 467,664,896 of an
+ * 8-byte type with 16-byte aligned pointers (233,832,448 / 116,916,224 with
+ * unaligned ones); larger n returns PP_ERR_WORKSPACE. All calls share the
+ * array: calls that overlap on the GPU race, so order them on one stream.
+ * The first call on each device looks up the array's address; make it
+ * outside stream capture. Device-side timeouts of this variant are not
+ * reported by pp_stream_status(). */
+pp_status pp_decoupled_scan_device_noalloc(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dtype,
+                                           const void* d_in, void* d_out, uint64_t n);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,124 @@
+// Allocation-free variant of the decoupled look-back scan entry point.
+//
+// Who needs it: some callers cannot allocate device memory at the moment they
+// run a scan. Code executing while a CUDA graph is being captured may not
+// call cudaMalloc; latency-critical loops must not enter the allocator, whose
+// calls can synchronise the whole device; and plug-ins hosted by a framework
+// that owns all device memory through its own pool are not allowed to create
+// allocations behind its back. The regular entry points take their scratch
+// (workspace header plus look-back descriptors) from a per-stream cache that
+// grows with cudaMallocAsync, or from a buffer the caller passes in; this one
+// takes it from a fixed array compiled into the library's device image, so it
+// allocates nothing at all.
+//
+// Limits and rules:
+//   * the scratch holds kNoAllocScratchBytes = 1 MiB, enough for 114,176
+//     descriptor words: up to 1,870,659,584 elements of a 4-byte type and
+//     467,664,896 of an 8-byte type with 16-byte aligned pointers (64 KB
+//     tiles), or 233,832,448 / 116,916,224 elements with unaligned pointers
+//     (2048-element tiles). Larger n is rejected with PP_ERR_WORKSPACE before
+//     anything is launched;
+//   * every GPU that loads the library holds the 1 MiB until the process
+//     exits;
+//   * all calls share the one array, which keeps the last call's contents.
+//     Each call therefore clears the part it uses (cudaMemsetAsync on the
+//     stream, no allocation) before its kernel. Calls that overlap on the GPU
+//     (on different streams, or from different threads without ordering)
+//     race on the array and give wrong results: order them on one stream;
+//   * the first call on each device looks up the array's device address with
+//     cudaGetSymbolAddress (once per device, with that device current); make
+//     that first call outside any stream capture;
+//   * a device-side timeout is recorded in the shared scratch only and is not
+//     reported by pp_stream_status(); callers that need that status use
+//     pp_scan_ws() with their own workspace.
+#include <cstdint>
+#include <mutex>
+
+#include <cuda_runtime.h>
+
+#include "dispatch.cuh"
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(1) << 20;
+
+// Host code must never use this name as an address: on the host it is only a
+// stand-in for the device symbol. The device address comes from
+// cudaGetSymbolAddress below.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void* g_scratch_addr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device (looked up once).
+pp_status scratch_address(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return PP_ERR_NO_DEVICE;
+  if (dev < 0 || dev >= kMaxDevices) return PP_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> g(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return PP_ERR_CUDA;
+    g_scratch_addr[dev] = p;
+  }
+  *out = g_scratch_addr[dev];
+  return PP_OK;
+}
+
+}  // namespace
+
+extern "C" pp_status pp_decoupled_scan_device_noalloc(pp_stream stream, pp_scan_kind kind, pp_op op,
+                                                      pp_dtype dtype, const void* d_in, void* d_out, uint64_t n) {
+  if (kind != PP_SCAN_INCLUSIVE && kind != PP_SCAN_EXCLUSIVE) return PP_ERR_INVALID_ARG;
+  if (op < PP_OP_PLUS || op > PP_OP_MAXIMUM || dtype < PP_I32 || dtype > PP_F64) return PP_ERR_INVALID_ARG;
+  if (n > 0 && (!d_in || !d_out)) return PP_ERR_INVALID_ARG;
+  const bool is_float = dtype == PP_F32 || dtype == PP_F64;
+  if (is_float && (op == PP_OP_BIT_AND || op == PP_OP_BIT_OR || op == PP_OP_BIT_XOR)) return PP_ERR_UNSUPPORTED;
+  if (n == 0) return PP_OK;
+
+  size_t need = 0;
+  pp_status st = pp_workspace_size(PP_ALGO_DECOUPLED, dtype, PP_PREC_DEFAULT, d_in, d_out, n, &need);
+  if (st != PP_OK) return st;
+  if (need > kNoAllocScratchBytes) return PP_ERR_WORKSPACE;
+
+  void* scratch = nullptr;
+  st = scratch_address(&scratch);
+  if (st != PP_OK) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // the previous call's header and descriptors must not leak into this one
+  if (cudaMemsetAsync(scratch, 0, need, s) != cudaSuccess) return PP_ERR_CUDA;
+
+  pp::capi::ScanReq r;
+  r.s = s;
+  r.exclusive = kind == PP_SCAN_EXCLUSIVE;
+  r.op = op;
+  r.in = d_in;
+  r.out = d_out;
+  r.n = n;
+  r.algo = PP_ALGO_DECOUPLED;
+  r.ws = scratch;
+  r.ws_bytes = kNoAllocScratchBytes;
+  pp::host::Status hs = pp::host::Status::invalid_arg;
+  switch (dtype) {
+    case PP_I32:
+      hs = pp::capi::scan_typed<int32_t>(r);
+      break;
+    case PP_U32:
+      hs = pp::capi::scan_typed<uint32_t>(r);
+      break;
+    case PP_I64:
+      hs = pp::capi::scan_typed<int64_t>(r);
+      break;
+    case PP_U64:
+      hs = pp::capi::scan_typed<uint64_t>(r);
+      break;
+    case PP_F32:
+      hs = pp::capi::scan_typed<float>(r);
+      break;
+    case PP_F64:
+      hs = pp::capi::scan_typed<double>(r);
+      break;
+  }
+  return static_cast<pp_status>(static_cast<int>(hs));
+}

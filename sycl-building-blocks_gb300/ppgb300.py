@@ -47,7 +47,7 @@ EXPORTS = [
     "pp_scan_device", "pp_group_scan_device", "pp_reduce_device", "pp_reduce", "pp_reduce_ws",
     "pp_decoupled_scan_host", "pp_cooperative_scan_host", "pp_scan_host", "pp_reduce_host", "pp_status_string",
     "pp_stream_status", "pp_workspace_status", "pp_set_timeout_ns", "pp_set_max_ctas", "pp_debug_set_skip_tile",
-    "pp_version", "pp_segmented_scan", "pp_segmented_reduce", "pp_rows_scan",
+    "pp_version", "pp_decoupled_scan_device_noalloc", "pp_segmented_scan", "pp_segmented_reduce", "pp_rows_scan",
 ]
 
 
@@ -73,7 +73,7 @@ def lib() -> C.CDLL:
     L.pp_scan_ws.argtypes = [vp, i32, i32, i32, vp, vp, u64, i32, i32, vp, sz]
     L.pp_workspace_size.argtypes = [i32, i32, i32, vp, vp, u64, C.POINTER(sz)]
     for name in ("pp_decoupled_scan_device", "pp_cooperative_scan_device", "pp_scan_device",
-                 "pp_group_scan_device"):
+                 "pp_group_scan_device", "pp_decoupled_scan_device_noalloc"):
         getattr(L, name).argtypes = [vp, i32, i32, i32, vp, vp, u64]
     L.pp_reduce_device.argtypes = [vp, i32, i32, vp, u64, vp]
     L.pp_reduce.argtypes = [vp, i32, i32, vp, u64, vp]
@@ -154,6 +154,13 @@ def workspace_size(algo, dtype, d_in: int, d_out: int, n: int, precision="defaul
 def decoupled_scan_device(kind, op, d_in: int, d_out: int, n: int, dtype, stream: int = 0) -> None:
     _check(lib().pp_decoupled_scan_device(stream, _kind(kind), _op(op), _dt(dtype), d_in, d_out, n),
            "pp_decoupled_scan_device")
+
+
+def decoupled_scan_device_noalloc(kind, op, d_in: int, d_out: int, n: int, dtype, stream: int = 0) -> None:
+    """The decoupled scan with the library's fixed device scratch instead of an
+    allocated workspace (for callers that may not allocate device memory)."""
+    _check(lib().pp_decoupled_scan_device_noalloc(stream, _kind(kind), _op(op), _dt(dtype), d_in, d_out, n),
+           "pp_decoupled_scan_device_noalloc")
 
 
 def cooperative_scan_device(kind, op, d_in: int, d_out: int, n: int, dtype, stream: int = 0) -> None:
