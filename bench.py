@@ -444,7 +444,7 @@ def bench_segmented(torch, pp, stream, steps) -> dict:
         ms_p, _ = time_device(torch, graph2.replay, max(2, steps // 20), 1, torch.cuda.current_stream())
         if pp.stream_status(s.cuda_stream) != 0:
             raise RuntimeError("device error in segmented benchmark")
-        res[dt] = {"batched_elems_per_s": round(n / (ms_b * 1e-3), 1), "batched_ms": round(ms_b / steps, 4),
+        res[dt] = {"batched_elems_per_s": round(n * steps / (ms_b * 1e-3), 1), "batched_ms": round(ms_b / steps, 4),
                    "per_segment_launches_ms": round(ms_p / max(2, steps // 20), 3),
                    "speedup": round((ms_p / max(2, steps // 20)) / (ms_b / steps), 2),
                    "batched_gbs": round(2 * n * 4 / (ms_b / steps * 1e-3) / 1e9, 2), "spot_check": ok}

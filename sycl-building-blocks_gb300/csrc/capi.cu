@@ -33,12 +33,16 @@ size_t dtype_size(pp_dtype d) {
   }
 }
 
+// Element access needs pointers aligned to the element size.
+bool aligned_to(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
+
 // Validation that needs no GPU: enums, pointers, combinations.
 pp_status check_scan_args(pp_scan_kind kind, pp_op op, pp_dtype dt, const void* in, const void* out, uint64_t n,
                           pp_scan_algo algo, pp_precision prec) {
   if (!valid_kind(kind) || !valid_op(op) || !valid_dtype(dt) || !valid_algo(algo) || !valid_prec(prec))
     return PP_ERR_INVALID_ARG;
   if (n > 0 && (!in || !out)) return PP_ERR_INVALID_ARG;
+  if (n > 0 && (!aligned_to(in, dtype_size(dt)) || !aligned_to(out, dtype_size(dt)))) return PP_ERR_INVALID_ARG;
   if (is_float(dt) && is_bitop(op)) return PP_ERR_UNSUPPORTED;
   if (prec != PP_PREC_DEFAULT && (dt != PP_F32 || op != PP_OP_PLUS)) return PP_ERR_UNSUPPORTED;
   return PP_OK;
@@ -171,6 +175,7 @@ pp_status pp_scan_ws(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dty
 pp_status pp_workspace_size(pp_scan_algo algo, pp_dtype dtype, pp_precision precision, const void* d_in,
                             const void* d_out, uint64_t n, size_t* bytes) {
   if (!bytes || !valid_algo(algo) || !valid_dtype(dtype) || !valid_prec(precision)) return PP_ERR_INVALID_ARG;
+  if (!aligned_to(d_in, dtype_size(dtype)) || !aligned_to(d_out, dtype_size(dtype))) return PP_ERR_INVALID_ARG;
   using namespace pp::capi;
   if (precision != PP_PREC_DEFAULT) {
     if (dtype != PP_F32) return PP_ERR_UNSUPPORTED;
@@ -222,6 +227,8 @@ pp_status pp_group_scan_device(pp_stream stream, pp_scan_kind kind, pp_op op, pp
 
 pp_status pp_reduce(pp_stream stream, pp_op op, pp_dtype dtype, const void* d_in, uint64_t n, void* d_result) {
   if (!valid_op(op) || !valid_dtype(dtype) || !d_result || (n > 0 && !d_in)) return PP_ERR_INVALID_ARG;
+  if (!aligned_to(d_result, dtype_size(dtype)) || (n > 0 && !aligned_to(d_in, dtype_size(dtype))))
+    return PP_ERR_INVALID_ARG;
   if (is_float(dtype) && is_bitop(op)) return PP_ERR_UNSUPPORTED;
   return to_c(reduce_dispatch(static_cast<cudaStream_t>(stream), op, dtype, d_in, n, d_result, nullptr, 0));
 }
@@ -229,6 +236,8 @@ pp_status pp_reduce(pp_stream stream, pp_op op, pp_dtype dtype, const void* d_in
 pp_status pp_reduce_ws(pp_stream stream, pp_op op, pp_dtype dtype, const void* d_in, uint64_t n, void* d_result,
                        void* d_workspace, size_t workspace_bytes) {
   if (!valid_op(op) || !valid_dtype(dtype) || !d_result || !d_workspace || (n > 0 && !d_in))
+    return PP_ERR_INVALID_ARG;
+  if (!aligned_to(d_result, dtype_size(dtype)) || (n > 0 && !aligned_to(d_in, dtype_size(dtype))))
     return PP_ERR_INVALID_ARG;
   if (is_float(dtype) && is_bitop(op)) return PP_ERR_UNSUPPORTED;
   return to_c(reduce_dispatch(static_cast<cudaStream_t>(stream), op, dtype, d_in, n, d_result, d_workspace,
@@ -239,6 +248,7 @@ pp_status pp_reduce_device(pp_stream stream, pp_op op, pp_dtype dtype, const voi
                            void* h_result) {
   if (!h_result) return PP_ERR_INVALID_ARG;
   if (!valid_op(op) || !valid_dtype(dtype) || (n > 0 && !d_in)) return PP_ERR_INVALID_ARG;
+  if (n > 0 && !aligned_to(d_in, dtype_size(dtype))) return PP_ERR_INVALID_ARG;
   if (is_float(dtype) && is_bitop(op)) return PP_ERR_UNSUPPORTED;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   HostStaging& st = staging();

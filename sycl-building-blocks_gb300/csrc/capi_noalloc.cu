@@ -13,11 +13,10 @@
 //
 // Limits and rules:
 //   * the scratch holds kNoAllocScratchBytes = 1 MiB, enough for 114,176
-//     descriptor words: up to 1,870,659,584 elements of a 4-byte type and
-//     467,664,896 of an 8-byte type with 16-byte aligned pointers (64 KB
-//     tiles), or 233,832,448 / 116,916,224 elements with unaligned pointers
-//     (2048-element tiles). Larger n is rejected with PP_ERR_WORKSPACE before
-//     anything is launched;
+//     descriptor words: up to 1,870,659,581 elements of a 4-byte type and
+//     467,664,895 of an 8-byte type (64 KB tiles; 1,870,659,584 / 467,664,896
+//     when the input is 16-byte aligned). Larger n is rejected with
+//     PP_ERR_WORKSPACE before anything is launched;
 //   * every GPU that loads the library holds the 1 MiB until the process
 //     exits;
 //   * all calls share the one array, which keeps the last call's contents.

@@ -54,6 +54,7 @@ struct ScanArgs {
   uint64_t timeout_ns;
   long long debug_skip_tile;  // a tile that never publishes (timeout tests); -1 = off
   int exclusive;
+  int head;  // staged kernel: elements between the previous 16-byte boundary and in[0]
 };
 
 __host__ __device__ constexpr size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -258,6 +259,29 @@ struct StagedCfg {
   static constexpr size_t SMEM = OFF_BAR + 4 * STAGES * 8;
 };
 
+// Geometry of tile t in the staged kernel. The tile grid is shifted by `head`
+// phantom elements so that every tile starts on a 16-byte boundary of the
+// input: tile t covers global indices [t*TILE - head, (t+1)*TILE - head).
+// Positions [lo, valid) of the tile hold data; positions [blo, bhi) arrive by
+// bulk copy, the rest of the valid ones (the first partial chunk of tile 0 and
+// the last < 16 bytes of the array) are read from global memory directly.
+struct StagedGeom {
+  long long gbase;  // global index of tile position 0
+  int lo, valid, blo, bhi;
+};
+template <int TILE, int V, int ESZ>
+__device__ __forceinline__ StagedGeom staged_geom(long long t, uint64_t n, int head) {
+  StagedGeom g;
+  g.gbase = t * TILE - head;
+  g.lo = t == 0 ? head : 0;
+  const long long end = (long long)n - g.gbase;
+  g.valid = end < TILE ? int(end) : TILE;
+  g.blo = (t == 0 && head > 0) ? V : 0;
+  const int span = g.valid > g.blo ? g.valid - g.blo : 0;
+  g.bhi = g.blo + int((uint32_t(span * ESZ) & ~15u) / ESZ);
+  return g;
+}
+
 // Warp-wide look-back reading LBW windows of 32 descriptors per round trip.
 template <class Pol, int LBW>
 __device__ __forceinline__ bool lookback_multi(const Pol& pol, const uint64_t* desc, long long tile,
@@ -368,7 +392,8 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const uint64_t n = args.n;
-  const long long ntiles = (long long)((n + TILE - 1) / TILE);
+  const int head = args.head;
+  const long long ntiles = (long long)((n + head + TILE - 1) / TILE);
   WsHeader* hdr = args.hdr;
   const uint64_t tmo = args.timeout_ns;
 
@@ -400,12 +425,12 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
         }
         *s_tile(s) = t;
         if (t < ntiles) {
-          const uint64_t base = uint64_t(t) * TILE;
-          const uint64_t valid = (n - base < uint64_t(TILE)) ? (n - base) : uint64_t(TILE);
-          const uint32_t bytes = uint32_t(valid * sizeof(in_t)) & ~15u;
+          const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(t, n, head);
+          const uint32_t bytes = uint32_t(g.bhi - g.blo) * uint32_t(sizeof(in_t));
           if (bytes) {
             ptx::mbar_arrive_expect_tx(&full[s], bytes);
-            ptx::bulk_g2s(smem + size_t(s) * Cfg::TILE_BYTES, in + base * sizeof(in_t), bytes, &full[s], pol_l2);
+            ptx::bulk_g2s(smem + size_t(s) * Cfg::TILE_BYTES + size_t(g.blo) * sizeof(in_t),
+                          in + (g.gbase + g.blo) * (long long)sizeof(in_t), bytes, &full[s], pol_l2);
             pending |= 1u << s;
             pend_par = (pend_par & ~(1u << s)) | ((uint32_t(k / STAGES) & 1u) << s);
           } else {
@@ -472,11 +497,12 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
     const bool excl_kind = args.exclusive != 0;
     auto aop = [&](const acc_t& x, const acc_t& y) { return pol.aop(x, y); };
 
+    const bool out_vec = ((reinterpret_cast<uintptr_t>(gout) - uintptr_t(head) * sizeof(out_t)) & 15u) == 0;
     // chunk c of this lane: V elements at tile offset w*SEG + (c*32 + lane)*V
-    auto load_chunk = [&](int s, int c, uint64_t base, int valid, int bulk, acc_t (&a)[V]) {
+    auto load_chunk = [&](int s, int c, const StagedGeom& g, acc_t (&a)[V]) {
       const unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
       const int e0 = w * Cfg::SEG + (c * 32 + lane) * V;
-      if (e0 + V <= bulk) {
+      if (e0 >= g.blo && e0 + V <= g.bhi) {
         union {
           uint4 u;
           in_t x[V];
@@ -488,12 +514,12 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
 #pragma unroll
         for (int j = 0; j < V; ++j) {
           const int e = e0 + j;
-          if (e < bulk)
-            a[j] = pol.load(reinterpret_cast<const in_t*>(stage)[e]);
-          else if (e < valid)
-            a[j] = pol.load(gin[base + e]);
-          else
+          if (e < g.lo || e >= g.valid)
             a[j] = pol.aid();
+          else if (e >= g.blo && e < g.bhi)
+            a[j] = pol.load(reinterpret_cast<const in_t*>(stage)[e]);
+          else
+            a[j] = pol.load(gin[g.gbase + e]);
         }
       }
     };
@@ -503,24 +529,27 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
       if (!mbar_wait_bounded(&full[s], (k / STAGES) & 1, hdr, tmo, 0ull)) return false;
       const long long tile = *s_tile(s);
       if (tile >= ntiles) return false;
-      const uint64_t base = uint64_t(tile) * TILE;
-      const uint64_t rem = n - base;
-      const int valid = rem < uint64_t(TILE) ? int(rem) : TILE;
-      const int bulk = int((uint32_t(valid * sizeof(in_t)) & ~15u) / sizeof(in_t));
+      const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(tile, n, head);
       acc_t r = pol.aid();
       if constexpr (pol_commutative<Pol>::value) {
+        // V independent accumulators: short dependency chains
+        acc_t rv[V];
+#pragma unroll
+        for (int j = 0; j < V; ++j) rv[j] = pol.aid();
 #pragma unroll 4
         for (int c = 0; c < CH; ++c) {
           acc_t a[V];
-          load_chunk(s, c, base, valid, bulk, a);
+          load_chunk(s, c, g, a);
 #pragma unroll
-          for (int j = 0; j < V; ++j) r = pol.aop(r, a[j]);
+          for (int j = 0; j < V; ++j) rv[j] = pol.aop(rv[j], a[j]);
         }
+#pragma unroll
+        for (int j = 0; j < V; ++j) r = pol.aop(r, rv[j]);
         r = warp_reduce(r, aop, lane);
       } else {
         for (int c = 0; c < CH; ++c) {
           acc_t a[V];
-          load_chunk(s, c, base, valid, bulk, a);
+          load_chunk(s, c, g, a);
           acc_t t = a[0];
 #pragma unroll
           for (int j = 1; j < V; ++j) t = pol.aop(t, a[j]);
@@ -563,38 +592,48 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
       if (!mbar_wait_bounded(&prefb[s], (k / STAGES) & 1, hdr, tmo, 0ull)) break;
       const long long tile = *s_tile(s);
       if (w == 0 && lane == 0) trace(kTrSStart, tile, ptx::globaltimer_ns());
-      const uint64_t base = uint64_t(tile) * TILE;
-      const uint64_t rem = n - base;
-      const int valid = rem < uint64_t(TILE) ? int(rem) : TILE;
-      const int bulk = int((uint32_t(valid * sizeof(in_t)) & ~15u) / sizeof(in_t));
+      const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(tile, n, head);
       // exclusive prefix of this warp's segment inside the tile
       acc_t sx = (lane < w) ? s_aggs(s)[lane] : pol.aid();
       sx = warp_reduce(sx, aop, lane);
       const pre_t pw = pol.prepare(w == 0 ? *s_pref(s) : pol.cop(*s_pref(s), pol.to_carry(sx)));
       acc_t X = pol.aid();
-#pragma unroll 2
-      for (int c = 0; c < CH; ++c) {
-        acc_t a[V];
-        load_chunk(s, c, base, valid, bulk, a);
+      // chunks in groups of SG: the SG warp scans of a group are independent
+      // and interleave, hiding shuffle and arithmetic latency
+      constexpr int SG = CH < 4 ? CH : 4;
+#pragma unroll 1
+      for (int c0 = 0; c0 < CH; c0 += SG) {
+        acc_t a[SG][V];
+        acc_t inc[SG];
 #pragma unroll
-        for (int j = 1; j < V; ++j) a[j] = pol.aop(a[j - 1], a[j]);
-        const acc_t inc = warp_inclusive_scan(a[V - 1], aop, lane);
-        acc_t ex = shfl_up(inc, 1);
-        if (lane == 0) ex = pol.aid();
-        const pre_t pc = pol.extend(pw, c == 0 ? ex : pol.aop(X, ex));
-        X = (c == 0) ? shfl_idx(inc, 31) : pol.aop(X, shfl_idx(inc, 31));
-        union {
-          uint4 u;
-          out_t x[V];
-        } o;
-        TileScan<Pol, NC, CH, V>::finish_chunk(pol, pc, a, excl_kind, o.x);
-        const int e0 = w * Cfg::SEG + (c * 32 + lane) * V;
-        if (e0 + V <= valid) {
-          ptx::st_stream_v4(gout + base + e0, o.u);
-        } else {
+        for (int q = 0; q < SG; ++q) {
+          load_chunk(s, c0 + q, g, a[q]);
 #pragma unroll
-          for (int j = 0; j < V; ++j)
-            if (e0 + j < valid) gout[base + e0 + j] = o.x[j];
+          for (int j = 1; j < V; ++j) a[q][j] = pol.aop(a[q][j - 1], a[q][j]);
+          inc[q] = a[q][V - 1];
+        }
+#pragma unroll
+        for (int q = 0; q < SG; ++q) inc[q] = warp_inclusive_scan(inc[q], aop, lane);
+#pragma unroll
+        for (int q = 0; q < SG; ++q) {
+          const int c = c0 + q;
+          acc_t ex = shfl_up(inc[q], 1);
+          if (lane == 0) ex = pol.aid();
+          const pre_t pc = pol.extend(pw, c == 0 ? ex : pol.aop(X, ex));
+          X = (c == 0) ? shfl_idx(inc[q], 31) : pol.aop(X, shfl_idx(inc[q], 31));
+          union {
+            uint4 u;
+            out_t x[V];
+          } o;
+          TileScan<Pol, NC, CH, V>::finish_chunk(pol, pc, a[q], excl_kind, o.x);
+          const int e0 = w * Cfg::SEG + (c * 32 + lane) * V;
+          if (out_vec && e0 >= g.lo && e0 + V <= g.valid) {
+            ptx::st_stream_v4(gout + (g.gbase + e0), o.u);
+          } else {
+#pragma unroll
+            for (int j = 0; j < V; ++j)
+              if (e0 + j >= g.lo && e0 + j < g.valid) gout[g.gbase + e0 + j] = o.x[j];
+          }
         }
       }
       __syncwarp();

@@ -225,39 +225,58 @@ template <class Pol>
 using StagedFor = StagedCfg<Pol, DecoupledTuning<Pol>::NC, DecoupledTuning<Pol>::CH, DecoupledTuning<Pol>::STAGES,
                             DecoupledTuning<Pol>::LBW>;
 
+// The staged (bulk-copy) kernel takes any naturally aligned pointers of an
+// element type whose size divides 16 bytes; the tile grid is shifted so that
+// tile starts fall on 16-byte boundaries of the input.
 template <class Pol>
 inline bool tma_path_ok(const void* in, const void* out) {
   using in_t = typename Pol::in_t;
   if constexpr (16 % sizeof(in_t) != 0 || sizeof(typename Pol::out_t) != sizeof(in_t)) {
     return false;
   } else {
-    return ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u) == 0;
+    return ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) % sizeof(in_t)) == 0;
   }
 }
 
+// Phantom elements in front of `in` up to the previous 16-byte boundary.
 template <class Pol>
-inline uint64_t decoupled_tile_elems(const void* in, const void* out) {
+inline int staged_head(const void* in) {
+  return int((reinterpret_cast<uintptr_t>(in) & 15u) / sizeof(typename Pol::in_t));
+}
+
+template <class Pol>
+inline uint64_t decoupled_tiles(uint64_t n, const void* in, const void* out) {
   using Tn = DecoupledTuning<Pol>;
   if constexpr (16 % sizeof(typename Pol::in_t) == 0) {
-    if (tma_path_ok<Pol>(in, out)) return StagedFor<Pol>::TILE;
+    if (tma_path_ok<Pol>(in, out)) {
+      const uint64_t tile = StagedFor<Pol>::TILE;
+      return (n + uint64_t(staged_head<Pol>(in)) + tile - 1) / tile;
+    }
   }
-  return DecoupledGenericCfg<Pol, Tn::GEN_NC, Tn::GEN_IPT>::TILE;
+  const uint64_t tile = DecoupledGenericCfg<Pol, Tn::GEN_NC, Tn::GEN_IPT>::TILE;
+  return (n + tile - 1) / tile;
 }
 
 template <class Pol>
 inline size_t decoupled_workspace_bytes(uint64_t n, const void* in, const void* out) {
-  const uint64_t tile = decoupled_tile_elems<Pol>(in, out);
-  const uint64_t ntiles = (n + tile - 1) / tile;
-  return workspace_bytes_for_desc_words(ntiles * desc_codec<typename Pol::carry_t>::W);
+  return workspace_bytes_for_desc_words(decoupled_tiles<Pol>(n, in, out) * desc_codec<typename Pol::carry_t>::W);
+}
+
+// Pointers must be aligned to the element type (element loads and stores).
+template <class T>
+inline bool type_aligned(const void* p) {
+  return (reinterpret_cast<uintptr_t>(p) % alignof(T)) == 0;
 }
 
 // grid_ctas: 0 = persistent grid (occupancy x SMs); otherwise the CTA count
-// (1 gives the single work-group scan of scan.hpp:125-130).
+// (1 gives the single work-group scan of scan.hpp:125-130). Element types
+// whose size does not divide 16 bytes take the register-tile kernel.
 template <class Pol>
 inline Status decoupled_scan(cudaStream_t s, const void* in, void* out, uint64_t n, bool exclusive,
                              void* user_ws = nullptr, size_t user_ws_bytes = 0, int grid_ctas = 0) {
   if (n == 0) return Status::ok;
   if (!in || !out) return Status::invalid_arg;
+  if (!type_aligned<typename Pol::in_t>(in) || !type_aligned<typename Pol::out_t>(out)) return Status::invalid_arg;
   using Tn = DecoupledTuning<Pol>;
   DeviceInfo di;
   Status st = device_info(di);
@@ -274,6 +293,7 @@ inline Status decoupled_scan(cudaStream_t s, const void* in, void* out, uint64_t
   a.timeout_ns = settings().timeout_ns.load();
   a.debug_skip_tile = settings().debug_skip_tile.load();
   a.exclusive = exclusive ? 1 : 0;
+  a.head = 0;
   const int cap = grid_ctas > 0 ? grid_ctas : settings().max_ctas.load();
   if constexpr (16 % sizeof(typename Pol::in_t) == 0) {
     if (tma_path_ok<Pol>(in, out)) {
@@ -282,7 +302,8 @@ inline Status decoupled_scan(cudaStream_t s, const void* in, void* out, uint64_t
       int bps = 0;
       st = prepare_kernel(k, Cfg::THREADS, Cfg::SMEM, bps);
       if (st != Status::ok) return st;
-      const uint64_t ntiles = (n + Cfg::TILE - 1) / Cfg::TILE;
+      a.head = staged_head<Pol>(in);
+      const uint64_t ntiles = decoupled_tiles<Pol>(n, in, out);
       uint64_t grid = uint64_t(bps) * di.sm_count;
       if (cap > 0 && uint64_t(cap) < grid) grid = cap;
       if (ntiles < grid) grid = ntiles;
@@ -319,6 +340,7 @@ inline Status cooperative_scan(cudaStream_t s, const void* in, void* out, uint64
                                void* user_ws = nullptr, size_t user_ws_bytes = 0, int grid_ctas = 0) {
   if (n == 0) return Status::ok;
   if (!in || !out) return Status::invalid_arg;
+  if (!type_aligned<typename Pol::in_t>(in) || !type_aligned<typename Pol::out_t>(out)) return Status::invalid_arg;
   using Tn = CoopTuning<Pol>;
   using Cfg = CoopCfg<Pol, Tn::NC, Tn::CH>;
   DeviceInfo di;
@@ -369,6 +391,7 @@ template <class T, class Op>
 inline Status reduce(cudaStream_t s, const T* in, uint64_t n, T* d_result, void* user_ws = nullptr,
                      size_t user_ws_bytes = 0) {
   if (!d_result || (n > 0 && !in)) return Status::invalid_arg;
+  if (!type_aligned<T>(d_result) || (n > 0 && !type_aligned<T>(in))) return Status::invalid_arg;
   using Tn = ReduceTuning<T, Op>;
   DeviceInfo di;
   Status st = device_info(di);
@@ -491,6 +514,7 @@ inline Status segmented_scan(cudaStream_t s, const T* in, T* out, uint64_t n, co
   if (n == 0 || num_segments == 0) return Status::ok;
   if (!in || !out || !offsets) return Status::invalid_arg;
   if (!aligned16(in) || !aligned16(out)) return Status::invalid_arg;
+  if (reinterpret_cast<uintptr_t>(offsets) & 7u) return Status::invalid_arg;
   const SegWsLayout L = seg_ws_layout<T, Op>(n, num_segments, true, false);
   Ws w;
   Status st = acquire_ws(s, L.control_bytes, user_ws, user_ws_bytes, w);
@@ -523,6 +547,7 @@ inline Status segmented_reduce(cudaStream_t s, const T* in, uint64_t n, const in
   if (num_segments == 0) return Status::ok;
   if (!offsets || !out || (n > 0 && !in)) return Status::invalid_arg;
   if (n > 0 && !aligned16(in)) return Status::invalid_arg;
+  if (!type_aligned<T>(out) || (reinterpret_cast<uintptr_t>(offsets) & 7u)) return Status::invalid_arg;
   const SegWsLayout L = seg_ws_layout<T, Op>(n, num_segments, true, true);
   Ws w;
   Status st = acquire_ws(s, L.control_bytes, user_ws, user_ws_bytes, w);

@@ -81,8 +81,7 @@ __global__ void __launch_bounds__(BLOCK) reduce_kernel(const ReduceArgs args) {
   uint64_t head = 0, nv = 0;
   if constexpr (V > 1) {
     const uintptr_t addr = reinterpret_cast<uintptr_t>(in);
-    head = ((16u - (addr & 15u)) & 15u) / sizeof(T);
-    if ((addr % sizeof(T)) != 0) head = n;  // not naturally aligned: scalar path only
+    head = ((16u - (addr & 15u)) & 15u) / sizeof(T);  // the host guarantees addr % sizeof(T) == 0
     if (head > n) head = n;
     nv = (n - head) / V;
     const uint4* vin = reinterpret_cast<const uint4*>(in + head);

@@ -56,6 +56,21 @@ __device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& 
   s = __fadd_rn(a, b);
   e = __fsub_rn(b, __fsub_rn(s, a));
 }
+// Pair + pair without renormalisation: hi carries the rounded sum of the high
+// parts, lo collects the low parts and the exact rounding error of hi. The
+// pair stays an exact-up-to-u*|lo| representation; |lo| grows by at most half
+// an ulp of hi per addition, so chains of a few dozen additions (tile scans)
+// stay far from overflowing lo's significance. Renormalise with ff_norm.
+__device__ __forceinline__ ff32 ff_add_lazy(const ff32& x, const ff32& y) {
+  float s, e;
+  two_sum(x.hi, y.hi, s, e);
+  return ff32{s, __fadd_rn(e, __fadd_rn(x.lo, y.lo))};
+}
+__device__ __forceinline__ ff32 ff_norm(const ff32& x) {
+  ff32 r;
+  fast_two_sum(x.hi, x.lo, r.hi, r.lo);
+  return r;
+}
 // Pair + pair ("sloppy" double-word addition): absolute error O(u^2 (|x|+|y|)).
 __device__ __forceinline__ ff32 ff_add(const ff32& x, const ff32& y) {
   float s, e;
@@ -75,6 +90,8 @@ __device__ __forceinline__ ff32 ff_add_f(const ff32& x, float y) {
   return r;
 }
 
+// In-tile pairs are added lazily (no renormalisation, ff_add_lazy); pairs are
+// renormalised when they become carries (descriptors, prefixes).
 struct CompensatedF32 {
   using in_t = float;
   using out_t = float;
@@ -83,13 +100,13 @@ struct CompensatedF32 {
   using pre_t = ff32;
 
   __device__ __forceinline__ acc_t load(const float& x) const { return ff32{x, 0.0f}; }
-  __device__ __forceinline__ acc_t aop(const acc_t& a, const acc_t& b) const { return ff_add(a, b); }
+  __device__ __forceinline__ acc_t aop(const acc_t& a, const acc_t& b) const { return ff_add_lazy(a, b); }
   __device__ __forceinline__ acc_t aid() const { return ff32{0.0f, 0.0f}; }
-  __device__ __forceinline__ carry_t to_carry(const acc_t& a) const { return a; }
+  __device__ __forceinline__ carry_t to_carry(const acc_t& a) const { return ff_norm(a); }
   __device__ __forceinline__ carry_t cop(const carry_t& a, const carry_t& b) const { return ff_add(a, b); }
   __device__ __forceinline__ carry_t cid() const { return ff32{0.0f, 0.0f}; }
   __device__ __forceinline__ pre_t prepare(const carry_t& c) const { return c; }
-  __device__ __forceinline__ pre_t extend(const pre_t& p, const acc_t& a) const { return ff_add(p, a); }
+  __device__ __forceinline__ pre_t extend(const pre_t& p, const acc_t& a) const { return ff_norm(ff_add_lazy(p, a)); }
   __device__ __forceinline__ out_t finish(const pre_t& p, const acc_t& a) const {
     float s, e;
     two_sum(p.hi, a.hi, s, e);

@@ -252,7 +252,7 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
 
     // Loads logical chunk c of this lane (V consecutive sequence positions).
     // Returns the head bits of the V elements (bit j for element j).
-    auto load_chunk = [&](int s, int c, uint64_t base, int valid, int bulk, in_t (&x)[V]) -> uint32_t {
+    auto load_chunk = [&](int s, int c, uint64_t base, int valid, int bulk, uint64_t mt, in_t (&x)[V]) -> uint32_t {
       const unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
       const int e0 = w * Cfg::SEG + (c * 32 + lane) * V;  // logical tile offset
       uint32_t hb = 0;
@@ -296,40 +296,46 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
         hb = (word >> (e0 & 31)) & ((1u << V) - 1u);
         if (e0 + V > valid) hb &= (e0 >= valid) ? 0u : ((1u << (valid - e0)) - 1u);
       } else {
+        // rows of seg_len elements; mt = base % seg_len (one 64-bit modulo per tile)
+        const uint64_t len = seg_len;
+        // distance D(j) from the tile's base to the element's row boundary:
+        // forward  phys = base + e0 + j,          head iff (phys) % len == 0
+        // reverse  phys = base + span - 1 - e0 - j, head iff (phys + 1) % len == 0
+        //          (span = TILE for full tiles, valid for the partial one)
+        const uint64_t span = uint64_t(valid == TILE ? TILE : valid);
 #pragma unroll
         for (int j = 0; j < V; ++j) {
           const int e = e0 + j;
           if (e < valid) {
-            // global physical index of sequence position e
-            const uint64_t g = REVERSE ? (valid == TILE ? base + uint64_t(TILE - 1 - e) : base + uint64_t(valid - 1 - e))
-                                       : base + uint64_t(e);
-            // forward: a row starts at g % len == 0; reverse: at the row's last element
-            const bool h = REVERSE ? ((g + 1) % seg_len == 0) : (g % seg_len == 0);
-            hb |= uint32_t(h) << j;
+            const uint64_t off = REVERSE ? span - uint64_t(e) : uint64_t(e);  // < 2 * TILE
+            const uint64_t r = len > uint64_t(2 * TILE) ? (mt + off >= len ? mt + off - len : mt + off)
+                                                        : uint64_t(uint32_t(mt + off) % uint32_t(len));
+            hb |= uint32_t(r == 0) << j;
           }
         }
       }
       return hb;
     };
-    auto tile_geom = [&](int s, long long& tile, uint64_t& base, int& valid, int& bulk) {
+    auto tile_geom = [&](int s, long long& tile, uint64_t& base, int& valid, int& bulk, uint64_t& mt) {
       tile = *s_tile(s);
       base = uint64_t(phys(tile)) * TILE;
       const uint64_t rem = n - base;
       valid = rem < uint64_t(TILE) ? int(rem) : TILE;
       bulk = int((uint32_t(valid * sizeof(in_t)) & ~15u) / sizeof(in_t));
+      mt = Heads::kBitmap ? 0 : base % seg_len;
     };
     auto reduce_pass = [&](int k) -> bool {
       const int s = k % STAGES;
       if (!mbar_wait_bounded(&full[s], (k / STAGES) & 1, hdr, tmo, 0ull)) return false;
       long long tile;
-      uint64_t base;
+      uint64_t base, mt;
       int valid, bulk;
-      tile_geom(s, tile, base, valid, bulk);
+      tile_geom(s, tile, base, valid, bulk, mt);
       if (tile >= ntiles) return false;
       acc_t r = pol.aid();
       for (int c = 0; c < CH; ++c) {
         in_t x[V];
-        const uint32_t hb = load_chunk(s, c, base, valid, bulk, x);
+        const uint32_t hb = load_chunk(s, c, base, valid, bulk, mt, x);
         acc_t t = pol.load(x[0], hb & 1u);
 #pragma unroll
         for (int j = 1; j < V; ++j) t = pol.aop(t, pol.load(x[j], (hb >> j) & 1u));
@@ -364,16 +370,16 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
       const int s = k % STAGES;
       if (!mbar_wait_bounded(&prefb[s], (k / STAGES) & 1, hdr, tmo, 0ull)) break;
       long long tile;
-      uint64_t base;
+      uint64_t base, mt;
       int valid, bulk;
-      tile_geom(s, tile, base, valid, bulk);
+      tile_geom(s, tile, base, valid, bulk, mt);
       acc_t sx = (lane < w) ? s_aggs(s)[lane] : pol.aid();
       sx = warp_reduce(sx, aop, lane);
       const acc_t pw = w == 0 ? *s_pref(s) : pol.aop(*s_pref(s), sx);
       acc_t X = pol.aid();
       for (int c = 0; c < CH; ++c) {
         in_t x[V];
-        const uint32_t hb = load_chunk(s, c, base, valid, bulk, x);
+        const uint32_t hb = load_chunk(s, c, base, valid, bulk, mt, x);
         acc_t a[V];
         a[0] = pol.load(x[0], hb & 1u);
 #pragma unroll

@@ -47,6 +47,10 @@ def test_host_side_argument_checks(pp):
     assert L.pp_set_timeout_ns(0) == pp.PP_ERR_INVALID_ARG
     assert L.pp_set_max_ctas(-1) == pp.PP_ERR_INVALID_ARG
     assert L.pp_decoupled_scan_host(0, 0, 9, dummy, dummy, 5) == pp.PP_ERR_INVALID_ARG
+    # pointers not aligned to the element size
+    assert L.pp_scan(None, 0, 0, 1, dummy + 2, dummy, 10, 0, 0) == pp.PP_ERR_INVALID_ARG
+    assert L.pp_scan(None, 0, 0, 3, dummy, dummy + 4, 10, 0, 0) == pp.PP_ERR_INVALID_ARG
+    assert L.pp_reduce(None, 0, 1, dummy + 1, 10, dummy) == pp.PP_ERR_INVALID_ARG
 
 
 def test_status_strings_and_version(pp):
@@ -64,6 +68,11 @@ def test_workspace_size_is_host_only(pp):
     assert size == 4096 + 8192 * 16 + (n // 16384) * 8
     # uint64: 64 KB tiles, two words each
     assert pp.workspace_size("decoupled", "u64", a, a, n) == 4096 + 8192 * 16 + (n // 8192) * 16
-    # unaligned pointers take the generic kernel: 2048-element register tiles
-    assert pp.workspace_size("decoupled", "u32", a + 4, a, n) == 4096 + 8192 * 16 + (n // 2048) * 8
+    # 4-byte but not 16-byte aligned input: the staged kernel's grid shifts by the phantom elements
+    assert pp.workspace_size("decoupled", "u32", a + 4, a, n) == 4096 + 8192 * 16 + (n // 16384 + 1) * 8
+    # not even aligned to the element size: refused
+    import pytest
+
+    with pytest.raises(pp.PPError):
+        pp.workspace_size("decoupled", "u32", a + 1, a, n)
     assert pp.workspace_size("cooperative", "f32", a, a, n) == 4096 + 8192 * 16

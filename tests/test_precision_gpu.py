@@ -64,8 +64,8 @@ def test_precision_modes_small_and_ragged(pp, oracle, cuda, precision, n):
 
 @pytest.mark.parametrize("precision", ["compensated", "fp64_carry"])
 def test_precision_modes_other_paths(pp, oracle, cuda, precision):
-    """Unaligned pointers (generic kernel) and the cooperative scan honour the
-    precision mode too."""
+    """Pointers that are not 16-byte aligned (shifted tile grid) and the
+    cooperative scan honour the precision mode too."""
     n = 200003
     x = oracle.gen_f32_normal(3, n)
     want = oracle.scan_fp64(x)

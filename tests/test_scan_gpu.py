@@ -27,19 +27,20 @@ def _tiles(n):
     return (n + 1023) // 1024
 
 
-def _run(pp, cuda, x, dtype, op, excl, algo="auto", offset=0, inplace=False):
+def _run(pp, cuda, x, dtype, op, excl, algo="auto", offset=0, inplace=False, out_offset=None):
     n = x.size
+    out_offset = offset if out_offset is None else out_offset
     d_in = to_dev(cuda, np.concatenate([np.zeros(offset, dtype=x.dtype), x]))
     if inplace:
         d_out = d_in
     else:
-        d_out = empty_dev(cuda, n, NP[dtype], pad=offset)
+        d_out = empty_dev(cuda, n, NP[dtype], pad=out_offset)
     esz = x.dtype.itemsize
     stream = cuda.cuda.current_stream().cuda_stream
     pp.scan("exclusive" if excl else "inclusive", op, d_in.data_ptr() + offset * esz,
-            d_out.data_ptr() + offset * esz, n, dtype, stream=stream, algo=algo)
+            d_out.data_ptr() + out_offset * esz, n, dtype, stream=stream, algo=algo)
     assert pp.stream_status(stream) == 0
-    return from_dev(d_out, NP[dtype])[offset:]
+    return from_dev(d_out, NP[dtype])[out_offset:]
 
 
 @pytest.mark.parametrize("dtype,op", ALL)
@@ -59,13 +60,32 @@ def test_decoupled_sizes(pp, oracle, cuda, n, dtype):
         check_scan(_run(pp, cuda, x, dtype, "plus", excl), x, dtype, "plus", excl, _tiles(n))
 
 
-@pytest.mark.parametrize("dtype", ["u32", "i64", "f64"])
-@pytest.mark.parametrize("offset", [1, 3])
-def test_unaligned_pointers_take_generic_path(pp, oracle, cuda, dtype, offset):
-    n = 70001
-    x = make_input(dtype, "plus", n, seed=5 + offset)
+@pytest.mark.parametrize("dtype", ["u32", "i64", "f64", "f32"])
+@pytest.mark.parametrize("offset,out_offset", [(1, 1), (3, 3), (1, 2), (2, 0), (0, 3)])
+@pytest.mark.parametrize("n", [1, 2, 5, 16383, 70001])
+def test_element_aligned_pointers_shift_the_tile_grid(pp, oracle, cuda, dtype, offset, out_offset, n):
+    """Pointers aligned to the element size but not to 16 bytes stay on the
+    bulk-copy kernel (tile grid shifted by the phantom elements in front of
+    in[0]); an output with a different misalignment takes scalar stores."""
+    x = make_input(dtype, "plus", n, seed=5 + offset + n)
     for excl in (False, True):
-        check_scan(_run(pp, cuda, x, dtype, "plus", excl, offset=offset), x, dtype, "plus", excl, _tiles(n))
+        got = _run(pp, cuda, x, dtype, "plus", excl, offset=offset, out_offset=out_offset)
+        check_scan(got, x, dtype, "plus", excl, _tiles(n))
+
+
+@pytest.mark.parametrize("dtype", ["u32", "f64"])
+def test_pointers_not_aligned_to_the_element_are_rejected(pp, cuda, dtype):
+    """An element cannot be loaded from an address that is not a multiple of
+    its size: the call is refused on the host before anything is launched."""
+    d = cuda.zeros(4096, dtype=cuda.uint8, device="cuda")
+    for a, b in ((1, 0), (0, 2), (3, 3)):
+        with pytest.raises(pp.PPError) as e:
+            pp.scan("inclusive", "plus", d.data_ptr() + a, d.data_ptr() + 64 + b, 100, dtype)
+        assert e.value.status == pp.PP_ERR_INVALID_ARG
+    for a in (1, 2, 3):
+        with pytest.raises(pp.PPError) as e:
+            pp.reduce_device("plus", d.data_ptr() + a, 100, dtype)
+        assert e.value.status == pp.PP_ERR_INVALID_ARG
 
 
 @pytest.mark.parametrize("dtype", ["u32", "u64"])
