@@ -181,8 +181,9 @@ const char* pp_version(void);
  * the allocator, in plug-ins whose host framework owns all device memory).
  * Its scratch is a fixed 1 MiB array in the library's device image instead
  * of a cudaMalloc'd or per-stream cached workspace, so it allocates nothing.
- * Limit: n up to 1,870,659,581 elements of a 4-byte type or 467,664,895 of an
- * 8-byte type; larger n returns PP_ERR_WORKSPACE. All calls share the
+ * Limit: n up to 1,870,659,581 elements of a 4-byte integer type,
+ * 2,104,492,029 floats or 526,123,007 elements of an 8-byte type; larger n
+ * returns PP_ERR_WORKSPACE. All calls share the
  * array: calls that overlap on the GPU race, so order them on one stream.
  * The first call on each device looks up the array's address; make it
  * outside stream capture. Device-side timeouts of this variant are not

@@ -6,25 +6,26 @@
 //  * Tiles are handed out by an atomic ticket counter (not by block id), so
 //    every predecessor of a tile belongs to a CTA that is already running:
 //    forward progress holds for any grid size and residency.
-//  * decoupled_staged_kernel (16-byte aligned data): a persistent,
-//    warp-specialised kernel with one CTA per SM. Warp 0 is the producer: one
-//    lane takes tickets and streams whole 64 KB tiles into a ring of
-//    shared-memory stages with cp.async.bulk (completion on mbarriers). Warp 1
-//    publishes the tile aggregate and runs the look-back. The NC compute warps
-//    reduce tile k+1 out of shared memory while the look-back of tile k is in
-//    flight, then scan tile k (thread-serial inside each 16-byte chunk,
-//    shuffle Kogge-Stone across lanes, warp segments combined through shared
-//    memory) and write it with coalesced 16-byte streaming stores. Large
-//    tiles keep the number of tiles, and so the length of the look-back
-//    chain, small.
+//  * decoupled_staged_kernel (element-aligned data, element sizes dividing 16
+//    bytes): a persistent, warp-specialised kernel with one CTA per SM. Warp 0
+//    is the producer: one lane takes tickets and streams whole tiles (64-72
+//    KB) into a ring of shared-memory stages with cp.async.bulk (completion on
+//    mbarriers). Warp 1 runs the look-back and publishes the inclusive
+//    prefix. The NC compute warps reduce tile k+1 out of shared memory while
+//    the look-back of tile k is in flight (the last of them publishes the tile
+//    aggregate at once), then scan tile k and write it with coalesced 16-byte
+//    streaming stores. Large tiles keep the number of tiles, and so the
+//    length of the look-back chain, small.
 //  * decoupled_generic_kernel: register tiles with plain element loads for
-//    any alignment and any element type (user functors, packed structs).
-//  * Strategy choice of the reference (:143-174): the look-back warp peeks at
-//    the predecessor's descriptor when the tile arrives. If the predecessor's
-//    inclusive prefix is already there ("reduce-then-scan"), the tile
-//    publishes its own inclusive prefix straight away and skips the
-//    look-back. Otherwise ("scan-then-reduce") it publishes its aggregate,
-//    runs the look-back and then publishes the prefix.
+//    element types whose size does not divide 16 bytes (user functors, packed
+//    structs).
+//  * Strategy choice of the reference (:143-174), decided by the predecessor
+//    descriptors: when the nearest predecessor's inclusive prefix is already
+//    published the look-back ends after one read ("reduce-then-scan");
+//    otherwise the published aggregates are folded back to the nearest
+//    prefix ("scan-then-reduce"). In the staged kernel the look-back does
+//    not wait for the tile's own aggregate (published separately, as soon as
+//    the reduce pass ends), so both overlap.
 //  * The look-back is warp-wide: LBW windows of 32 predecessors per memory
 //    round trip, the nearest inclusive prefix found with ballots, the windows
 //    folded with ordered shuffle reductions (the reference walks one
@@ -63,17 +64,23 @@ __host__ __device__ constexpr size_t align_up(size_t x, size_t a) { return (x + 
 // tile's life with an event id, the tile index and a value. The default does
 // nothing and compiles away.
 struct NoTrace {
+  static constexpr bool kOn = false;
   __device__ __forceinline__ void operator()(int, long long, unsigned long long) const {}
 };
 enum TraceEvent : int {
   kTrFull = 0,     // look-back warp sees the tile in shared memory
   kTrAggPub = 1,   // last compute warp published the tile aggregate
-  kTrAgg = 2,      // look-back warp has the tile aggregate
-  kTrLbDone = 3,   // inclusive prefix published
+  kTrAgg = 2,      // look-back warp has the tile aggregate (publishes the prefix)
+  kTrLbDone = 3,   // look-back warp has the exclusive prefix
   kTrLbRounds = 4, // look-back rounds (value), spins in the upper half
   kTrSStart = 5,   // compute warp 0 starts the scan pass
   kTrSDone = 6,    // compute warp 0 finished the scan pass
-  kTrPeek = 7,     // 1 when the predecessor's prefix was there on arrival
+  kTrTicket = 9,   // producer drew the tile's ticket
+  kTrIssue = 10,   // producer issued the tile's bulk copy (its stage was free)
+  kTrRWait = 11,   // compute warp 0 starts waiting for the tile's data
+  kTrRGot = 12,    // compute warp 0 has the tile's data (reduce pass begins)
+  kTrPWait = 13,   // compute warp 0 starts waiting for the tile's prefix
+  kTrPollRt = 14,  // duration of the first look-back poll (ns)
 };
 
 // Warp-wide look-back for `tile`. On success writes the combination of the
@@ -232,11 +239,24 @@ struct pol_commutative<CompensatedF32> : std::true_type {};
 template <>
 struct pol_commutative<F64CarryF32> : std::true_type {};
 
-template <class Pol, int NC_, int CH_, int STAGES_, int LBW_>
+// LAY selects the layout of the passes over a tile:
+//   0 striped: chunk c of a warp's segment is 32 consecutive 16-byte chunks,
+//     one per lane; every chunk needs its own warp scan;
+//   1 lane-blocked: each lane owns a row of CH consecutive chunks; one warp
+//     scan per segment, chunk prefixes inside the row;
+//   2 rows: as 1, and the reduce pass leaves each row's total in shared
+//     memory, so the scan pass is one thread-serial chain along the row
+//     (Pol::row_incl / row_excl: one combine per element).
+// CH odd in layouts 1 and 2: rows of CH * 16 bytes then start in 8 different
+// 16-byte bank groups for any 8 consecutive lanes, so row reads are free of
+// bank conflicts; results go back into the row and leave striped.
+template <class Pol, int NC_, int CH_, int STAGES_, int LBW_, int LAY_ = 0, int NR_ = 0>
 struct StagedCfg {
   using in_t = typename Pol::in_t;
   using acc_t = typename Pol::acc_t;
   using carry_t = typename Pol::carry_t;
+  static constexpr int LAY = LAY_;
+  static_assert(LAY_ == 0 || (CH_ % 2) == 1, "lane rows need an odd chunk count");
   static constexpr int NC = NC_;            // compute warps
   static constexpr int CH = CH_;            // 16-byte chunks per lane per segment
   static constexpr int STAGES = STAGES_;    // shared-memory ring depth
@@ -246,17 +266,19 @@ struct StagedCfg {
   static constexpr int SEG = 32 * CH * V;   // elements per compute warp
   static constexpr int TILE = NC * SEG;
   static constexpr int TILE_BYTES = TILE * int(sizeof(in_t));
-  static constexpr int THREADS = (NC + 2) * 32;
+  static constexpr int NR = NR_;            // reducer warps (0: the compute warps reduce too)
+  static constexpr int THREADS = (NC + NR + 2) * 32;
   // per-stage metadata
   static constexpr size_t META_AGG = 0;                                   // acc_t[NC] segment aggregates
   static constexpr size_t META_PREF = align_up(NC * sizeof(acc_t), 16);   // carry_t tile exclusive prefix
   static constexpr size_t META_TAGG = META_PREF + align_up(sizeof(carry_t), 16);  // carry_t tile aggregate
   static constexpr size_t META_TILE = META_TAGG + align_up(sizeof(carry_t), 8);   // long long tile index
   static constexpr size_t META_CNT = META_TILE + 8;                                // unsigned arrivals
-  static constexpr size_t META_BYTES = align_up(META_CNT + 4, 16);
+  static constexpr size_t META_ROWS = align_up(META_CNT + 4, 16);                  // acc_t[NC*32] row totals
+  static constexpr size_t META_BYTES = align_up(META_ROWS + (LAY_ == 2 ? NC_ * 32 * sizeof(acc_t) : 0), 16);
   static constexpr size_t OFF_META = size_t(STAGES) * TILE_BYTES;
-  static constexpr size_t OFF_BAR = align_up(OFF_META + STAGES * META_BYTES, 8);  // 4 barriers / stage
-  static constexpr size_t SMEM = OFF_BAR + 4 * STAGES * 8;
+  static constexpr size_t OFF_BAR = align_up(OFF_META + STAGES * META_BYTES, 8);  // 5 barriers / stage
+  static constexpr size_t SMEM = OFF_BAR + 5 * STAGES * 8;
 };
 
 // Geometry of tile t in the staged kernel. The tile grid is shifted by `head`
@@ -361,9 +383,143 @@ __device__ __forceinline__ bool lookback_multi(const Pol& pol, const uint64_t* d
   return true;
 }
 
-template <class Pol, int NC, int CH, int STAGES, int LBW, class Trace = NoTrace>
-__global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(const ScanArgs args) {
-  using Cfg = StagedCfg<Pol, NC, CH, STAGES, LBW>;
+// Look-back with two polls in flight. Descriptors become visible one L2
+// round trip (about a microsecond while HBM streams at full rate) after they
+// are published; a poll that just misses a publication would add another
+// round trip. Here a second poll is issued GAP_NS after the first and each
+// evaluated poll is re-issued at once, so successive samples of the window
+// are about half a round trip apart.
+template <class Pol, int LBW, unsigned GAP_NS, bool TIMED = false>
+__device__ __forceinline__ bool lookback_pipelined(const Pol& pol, const uint64_t* desc, long long tile,
+                                                   uint32_t etag, WsHeader* hdr, uint64_t timeout_ns, int lane,
+                                                   typename Pol::carry_t& out, unsigned long long& stats,
+                                                   unsigned long long* first_rt = nullptr) {
+  using C = typename Pol::carry_t;
+  using codec = desc_codec<C>;
+  constexpr int W = codec::W;
+  auto cop = [&](const C& x, const C& y) { return pol.cop(x, y); };
+  C acc = pol.cid();
+  long long base = tile - 1;
+  unsigned rounds = 0, spin_total = 0, spins = 0;
+  uint64_t t0 = 0;
+  uint64_t ra[LBW][W], rb[LBW][W];
+  auto issue = [&](uint64_t (&r)[LBW][W]) {
+#pragma unroll
+    for (int j = 0; j < LBW; ++j) {
+      const long long t = base - lane - 32 * j;
+      if (t >= 0) codec::load_raw(desc + t * W, r[j]);
+    }
+  };
+  // 0: blocked (an unpublished predecessor before the nearest prefix),
+  // 1: done (acc holds the exclusive prefix), 2: folded all windows, go on
+  auto step = [&](const uint64_t (&r)[LBW][W]) -> int {
+    C v[LBW];
+    uint32_t st[LBW];
+#pragma unroll
+    for (int j = 0; j < LBW; ++j) {
+      const long long t = base - lane - 32 * j;
+      v[j] = pol.cid();
+      st[j] = kPrefix;
+      if (t >= 0) st[j] = codec::decode(r[j], etag, v[j]);
+    }
+    int pj = LBW, pl = 32;
+    bool blocked = false;
+#pragma unroll
+    for (int j = 0; j < LBW; ++j) {
+      const uint32_t pm = __ballot_sync(kFullMask, st[j] == kPrefix);
+      const uint32_t xm = __ballot_sync(kFullMask, st[j] == kInvalid);
+      if (pj == LBW) {
+        if (pm) {
+          const int p = __ffs(pm) - 1;
+          const uint32_t need = (p >= 31) ? kFullMask : ((2u << p) - 1u);
+          blocked |= (xm & need) != 0u;
+          pj = j;
+          pl = p;
+        } else {
+          blocked |= xm != 0u;
+        }
+      }
+    }
+    if (blocked) return 0;
+    ++rounds;
+#pragma unroll
+    for (int j = 0; j < LBW; ++j) {
+      if (j <= pj) {
+        C x = (j < pj || lane <= pl) ? v[j] : pol.cid();
+        x = warp_reduce_reversed(x, cop, lane);
+        acc = pol.cop(x, acc);
+      }
+    }
+    if (pj < LBW) return 1;
+    base -= 32 * LBW;
+    return 2;
+  };
+  // bounded spinning: false when the wait timed out or another CTA aborted
+  auto spin_ok = [&]() -> bool {
+    if (spins == 0) t0 = ptx::globaltimer_ns();
+    ++spins;
+    ++spin_total;
+    if ((spins & 7u) != 0u) return true;
+    bool give_up = false;
+    if (lane == 0) {
+      if (aborted(hdr)) {
+        give_up = true;
+      } else if (ptx::globaltimer_ns() - t0 > timeout_ns) {
+        raise_error(hdr, kDevTimeout, (unsigned long long)tile);
+        give_up = true;
+      }
+    }
+    return !__shfl_sync(kFullMask, give_up, 0);
+  };
+  const uint64_t t_first = TIMED ? ptx::globaltimer_ns() : 0ull;
+  issue(ra);
+  bool first = true;
+  while (true) {
+    ptx::nanosleep(GAP_NS);
+    issue(rb);
+    int x = step(ra);
+    if (TIMED && first) {
+      *first_rt = ptx::globaltimer_ns() - t_first;
+      first = false;
+    }
+    if (x == 1) break;
+    if (x == 2) {
+      spins = 0;
+      issue(ra);
+      continue;
+    }
+    if (!spin_ok()) return false;
+    issue(ra);
+    x = step(rb);
+    if (x == 1) break;
+    if (x == 2) {
+      spins = 0;
+      issue(ra);
+      continue;
+    }
+    if (!spin_ok()) return false;
+  }
+  out = acc;
+  stats = (unsigned long long)rounds | ((unsigned long long)spin_total << 32);
+  return true;
+}
+
+// NR: 0 = every compute warp runs the reduce pass of tile k+1 before the scan
+// pass of tile k; > 0 = NR dedicated reducer warps reduce tiles as soon as
+// they arrive (up to STAGES-1 ahead of the scan), so a late prefix never
+// delays the publication of the next aggregates.
+// PG: 0 = one look-back poll in flight; > 0 = two, the second PG ns later.
+// TK: when the producer draws the ticket of the next tile for a stage.
+//   0: right after issuing the previous copy (a full stage life ahead);
+//   1: when the compute warps start scanning the tile still in that stage;
+//   2: once the stage is free.
+// Later tickets make the order of tickets follow the order in which tiles
+// reach their reduce pass more closely, so predecessors' aggregates arrive
+// closer together; earlier ones hide the latency of the ticket atomic.
+template <class Pol, int NC, int CH, int STAGES, int LBW, int LAY = 0, int TK = 0, int NR = 0,
+          unsigned PG = 0, class Trace = NoTrace>
+__global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel(const ScanArgs args) {
+  using Cfg = StagedCfg<Pol, NC, CH, STAGES, LBW, LAY, NR>;
   using in_t = typename Pol::in_t;
   using out_t = typename Pol::out_t;
   using acc_t = typename Pol::acc_t;
@@ -380,15 +536,21 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
   uint64_t* empty = bars + STAGES;
   uint64_t* aggb = bars + 2 * STAGES;
   uint64_t* prefb = bars + 3 * STAGES;
+  uint64_t* sgo = bars + 4 * STAGES;  // compute warp 0 starts the scan pass (TK == 1)
   auto meta = [&](int s) { return smem + Cfg::OFF_META + size_t(s) * Cfg::META_BYTES; };
   auto s_aggs = [&](int s) { return reinterpret_cast<acc_t*>(meta(s) + Cfg::META_AGG); };
   auto s_pref = [&](int s) { return reinterpret_cast<carry_t*>(meta(s) + Cfg::META_PREF); };
   auto s_tagg = [&](int s) { return reinterpret_cast<carry_t*>(meta(s) + Cfg::META_TAGG); };
   auto s_tile = [&](int s) { return reinterpret_cast<long long*>(meta(s) + Cfg::META_TILE); };
   auto s_cnt = [&](int s) { return reinterpret_cast<unsigned*>(meta(s) + Cfg::META_CNT); };
+  auto s_rows = [&](int s) { return reinterpret_cast<acc_t*>(meta(s) + Cfg::META_ROWS); };
 
   const Pol pol{};
   const Trace trace{};
+  // timestamps are read only when a recording Trace is compiled in
+  auto trace_now = [&](int ev, long long tile) {
+    if constexpr (Trace::kOn) trace(ev, tile, ptx::globaltimer_ns());
+  };
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const uint64_t n = args.n;
@@ -401,8 +563,9 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
     for (int s = 0; s < STAGES; ++s) {
       ptx::mbar_init(&full[s], 1);
       ptx::mbar_init(&empty[s], NC);
-      ptx::mbar_init(&aggb[s], NC);
+      ptx::mbar_init(&aggb[s], NR > 0 ? NR : NC);
       ptx::mbar_init(&prefb[s], 1);
+      ptx::mbar_init(&sgo[s], 1);
       *s_cnt(s) = 0u;
     }
     ptx::fence_mbar_init();
@@ -416,15 +579,29 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
       const uint64_t pol_l2 = ptx::policy_evict_first();
       const unsigned char* in = static_cast<const unsigned char*>(args.in);
       uint32_t pending = 0, pend_par = 0;
-      long long t = (long long)atomicAdd(&hdr->ticket, 1ull);
+      auto draw = [&]() {
+        const long long x = (long long)atomicAdd(&hdr->ticket, 1ull);
+        if (x < ntiles) trace_now(kTrTicket, x);
+        return x;
+      };
+      long long t = TK == 0 ? draw() : 0;
       for (int k = 0;; ++k) {
         const int s = k % STAGES;
         if (k >= STAGES) {
-          if (!mbar_wait_bounded(&empty[s], ((k / STAGES) - 1) & 1, hdr, tmo, (unsigned long long)t)) break;
+          const uint32_t par = ((k / STAGES) - 1) & 1;
+          if constexpr (TK == 1) {
+            if (!mbar_wait_bounded(&sgo[s], par, hdr, tmo, 0ull)) break;
+            t = draw();
+          }
+          if (!mbar_wait_bounded(&empty[s], par, hdr, tmo, (unsigned long long)t)) break;
+          if constexpr (TK == 2) t = draw();
           pending &= ~(1u << s);
+        } else if constexpr (TK != 0) {
+          t = draw();
         }
         *s_tile(s) = t;
         if (t < ntiles) {
+          trace_now(kTrIssue, t);
           const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(t, n, head);
           const uint32_t bytes = uint32_t(g.bhi - g.blo) * uint32_t(sizeof(in_t));
           if (bytes) {
@@ -436,7 +613,7 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
           } else {
             ptx::mbar_arrive(&full[s]);
           }
-          t = (long long)atomicAdd(&hdr->ticket, 1ull);
+          if constexpr (TK == 0) t = draw();
         } else {
           ptx::mbar_arrive(&full[s]);
           break;
@@ -454,35 +631,33 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
       if (!mbar_wait_bounded(&full[s], par, hdr, tmo, 0ull)) break;
       const long long tile = *s_tile(s);
       if (tile >= ntiles) break;
-      trace(kTrFull, tile, ptx::globaltimer_ns());
-      uint32_t peek_st = kInvalid;
-      carry_t peek_v = pol.cid();
-      if (lane == 0 && tile > 0) peek_st = codec::read(args.desc + (tile - 1) * codec::W, etag, peek_v);
-      if (!mbar_wait_bounded(&aggb[s], par, hdr, tmo, 0ull)) break;
-      trace(kTrAgg, tile, ptx::globaltimer_ns());
-      // the tile aggregate was published by the last compute warp of the reduce pass
-      const carry_t agg = *s_tagg(s);
-      uint64_t* d = args.desc + tile * codec::W;
-      const bool publish = tile != args.debug_skip_tile;
+      trace_now(kTrFull, tile);
+      // The exclusive prefix depends on the predecessors' descriptors only, so
+      // it is looked up while the compute warps still reduce this tile. The
+      // nearest predecessors decide the path: a published inclusive prefix
+      // ends the look-back at once (reduce-then-scan); published aggregates
+      // are combined back to the nearest prefix (scan-then-reduce).
       carry_t excl = pol.cid();
-      bool ok = true;
       unsigned long long stats = 0;
-      const bool ready = tile == 0 || __shfl_sync(kFullMask, peek_st, 0) == kPrefix;
-      if (tile == 0) {
-        // published as a prefix by the reduce pass
-      } else if (ready) {
-        // reduce-then-scan: predecessor prefix known on arrival
-        excl = shfl_idx(peek_v, 0);
-        if (lane == 0 && publish) codec::publish(d, pol.cop(excl, agg), make_tag(etag, kPrefix));
-      } else {
-        // scan-then-reduce: the aggregate is out, look back for the prefix
-        ok = lookback_multi<Pol, LBW>(pol, args.desc, tile, etag, hdr, tmo, lane, excl, stats);
-        if (ok && lane == 0 && publish) codec::publish(d, pol.cop(excl, agg), make_tag(etag, kPrefix));
+      if (tile > 0) {
+        bool ok;
+        unsigned long long rt = 0;
+        if constexpr (PG > 0)
+          ok = lookback_pipelined<Pol, LBW, PG, Trace::kOn>(pol, args.desc, tile, etag, hdr, tmo, lane, excl, stats,
+                                                           &rt);
+        else
+          ok = lookback_multi<Pol, LBW>(pol, args.desc, tile, etag, hdr, tmo, lane, excl, stats);
+        if (!ok) break;
+        trace(kTrPollRt, tile, rt);
       }
-      if (!ok) break;
-      trace(kTrLbDone, tile, ptx::globaltimer_ns());
+      trace_now(kTrLbDone, tile);
       trace(kTrLbRounds, tile, stats);
-      trace(kTrPeek, tile, ready ? 1ull : 0ull);
+      if (!mbar_wait_bounded(&aggb[s], par, hdr, tmo, 0ull)) break;
+      trace_now(kTrAgg, tile);
+      // the tile aggregate was published by the last compute warp of the
+      // reduce pass (tile 0: as its inclusive prefix)
+      if (tile > 0 && lane == 0 && tile != args.debug_skip_tile)
+        codec::publish(args.desc + tile * codec::W, pol.cop(excl, *s_tagg(s)), make_tag(etag, kPrefix));
       if (lane == 0) {
         *s_pref(s) = excl;
         ptx::mbar_arrive(&prefb[s]);
@@ -491,17 +666,18 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
     }
   } else {
     // ------------------------------------------------------------ compute
-    const int w = warp - 2;
+    // split mode: warps 2..NR+1 reduce, the NC warps after them scan
+    const bool reducer = NR > 0 && warp < 2 + NR;
+    const int w = NR > 0 ? (reducer ? warp - 2 : warp - 2 - NR) : warp - 2;
     const in_t* gin = static_cast<const in_t*>(args.in);
     out_t* gout = static_cast<out_t*>(args.out);
     const bool excl_kind = args.exclusive != 0;
     auto aop = [&](const acc_t& x, const acc_t& y) { return pol.aop(x, y); };
 
     const bool out_vec = ((reinterpret_cast<uintptr_t>(gout) - uintptr_t(head) * sizeof(out_t)) & 15u) == 0;
-    // chunk c of this lane: V elements at tile offset w*SEG + (c*32 + lane)*V
-    auto load_chunk = [&](int s, int c, const StagedGeom& g, acc_t (&a)[V]) {
+    // V elements at tile offset e0 (a 16-byte chunk of the stage)
+    auto load_at = [&](int s, int e0, const StagedGeom& g, acc_t (&a)[V]) {
       const unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
-      const int e0 = w * Cfg::SEG + (c * 32 + lane) * V;
       if (e0 >= g.blo && e0 + V <= g.bhi) {
         union {
           uint4 u;
@@ -523,15 +699,51 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
         }
       }
     };
-    // reduce pass of use k: returns false at the end of work or on a failed wait
-    auto reduce_pass = [&](int k) -> bool {
-      const int s = k % STAGES;
-      if (!mbar_wait_bounded(&full[s], (k / STAGES) & 1, hdr, tmo, 0ull)) return false;
-      const long long tile = *s_tile(s);
-      if (tile >= ntiles) return false;
-      const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(tile, n, head);
+    // V raw elements at tile offset e0, the identity outside the valid range
+    auto load_raw_at = [&](int s, int e0, const StagedGeom& g, bool interior, in_t (&x)[V]) {
+      const unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
+      if (interior || (e0 >= g.blo && e0 + V <= g.bhi)) {
+        union {
+          uint4 u;
+          in_t x[V];
+        } buf;
+        buf.u = *reinterpret_cast<const uint4*>(stage + size_t(e0) * sizeof(in_t));
+#pragma unroll
+        for (int j = 0; j < V; ++j) x[j] = buf.x[j];
+      } else {
+#pragma unroll
+        for (int j = 0; j < V; ++j) {
+          const int e = e0 + j;
+          if (e < g.lo || e >= g.valid)
+            x[j] = pol.in_id();
+          else if (e >= g.blo && e < g.bhi)
+            x[j] = reinterpret_cast<const in_t*>(stage)[e];
+          else
+            x[j] = gin[g.gbase + e];
+        }
+      }
+    };
+    // striped chunk c of this lane in segment seg: tile offset seg*SEG + (c*32 + lane)*V
+    auto load_chunk = [&](int s, int seg, int c, const StagedGeom& g, acc_t (&a)[V]) {
+      load_at(s, seg * Cfg::SEG + (c * 32 + lane) * V, g, a);
+    };
+    // aggregate of segment seg of stage s (a warp-wide value)
+    auto reduce_segment = [&](int s, int seg, const StagedGeom& g) -> acc_t {
       acc_t r = pol.aid();
-      if constexpr (pol_commutative<Pol>::value) {
+      if constexpr (LAY == 2) {
+        // this lane's row, in order; the row total stays for the scan pass
+        const int r0 = seg * Cfg::SEG + lane * (CH * V);
+        const bool interior = g.lo == 0 && g.blo == 0 && g.bhi == TILE;
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+          in_t x[V];
+          load_raw_at(s, r0 + c * V, g, interior, x);
+#pragma unroll
+          for (int j = 0; j < V; ++j) r = pol.aop_in(r, x[j]);
+        }
+        s_rows(s)[seg * 32 + lane] = r;
+        r = warp_reduce(r, aop, lane);
+      } else if constexpr (pol_commutative<Pol>::value) {
         // V independent accumulators: short dependency chains
         acc_t rv[V];
 #pragma unroll
@@ -539,7 +751,7 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
 #pragma unroll 4
         for (int c = 0; c < CH; ++c) {
           acc_t a[V];
-          load_chunk(s, c, g, a);
+          load_chunk(s, seg, c, g, a);
 #pragma unroll
           for (int j = 0; j < V; ++j) rv[j] = pol.aop(rv[j], a[j]);
         }
@@ -549,19 +761,23 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
       } else {
         for (int c = 0; c < CH; ++c) {
           acc_t a[V];
-          load_chunk(s, c, g, a);
+          load_chunk(s, seg, c, g, a);
           acc_t t = a[0];
 #pragma unroll
           for (int j = 1; j < V; ++j) t = pol.aop(t, a[j]);
           r = pol.aop(r, warp_reduce(t, aop, lane));
         }
       }
-      // the last compute warp to finish combines the segment aggregates and
-      // publishes the tile aggregate at once (tile 0: its inclusive prefix),
-      // so successors never wait for this CTA's look-back of an earlier tile
+      return r;
+    };
+    // Records the aggregate of segment seg. The warp that records the last
+    // segment of the tile combines them and publishes the tile aggregate at
+    // once (tile 0: its inclusive prefix), so successors never wait for this
+    // CTA's look-back of an earlier tile.
+    auto record_segment = [&](int s, int seg, long long tile, const acc_t& r) {
       unsigned last = 0;
       if (lane == 0) {
-        s_aggs(s)[w] = r;
+        s_aggs(s)[seg] = r;
         __threadfence_block();
         last = atomicAdd(s_cnt(s), 1u) == unsigned(NC - 1);
       }
@@ -575,28 +791,179 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
           *s_cnt(s) = 0u;
           if (tile != args.debug_skip_tile)
             codec::publish(args.desc + tile * codec::W, agg, make_tag(etag, tile == 0 ? kPrefix : kAggregate));
-          trace(kTrAggPub, tile, ptx::globaltimer_ns());
+          trace_now(kTrAggPub, tile);
         }
       }
       __syncwarp();
+    };
+    // reduce pass of use k over the segments of this warp: returns false at
+    // the end of work or on a failed wait
+    auto reduce_pass = [&](int k) -> bool {
+      const int s = k % STAGES;
+      const unsigned long long tw = Trace::kOn ? ptx::globaltimer_ns() : 0ull;
+      if (!mbar_wait_bounded(&full[s], (k / STAGES) & 1, hdr, tmo, 0ull)) return false;
+      const long long tile = *s_tile(s);
+      if (tile >= ntiles) return false;
+      if (w == 0 && lane == 0) {
+        trace(kTrRWait, tile, tw);
+        trace_now(kTrRGot, tile);
+      }
+      const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(tile, n, head);
+      if constexpr (NR > 0) {
+        for (int seg = w; seg < NC; seg += NR) record_segment(s, seg, tile, reduce_segment(s, seg, g));
+      } else {
+        record_segment(s, w, tile, reduce_segment(s, w, g));
+      }
       if (lane == 0) ptx::mbar_arrive(&aggb[s]);
       __syncwarp();
       return true;
     };
 
-    bool have = reduce_pass(0);
+    if (reducer) {
+      for (int k = 0; reduce_pass(k); ++k) {
+      }
+    }
+    bool have = NR > 0 ? !reducer : reduce_pass(0);
     for (int k = 0; have; ++k) {
-      const bool have_next = reduce_pass(k + 1);
-      // scan pass of use k
+      bool have_next = true;
       const int s = k % STAGES;
+      if constexpr (NR > 0) {
+        // the end of work shows in the tile index of the stage
+        if (!mbar_wait_bounded(&full[s], (k / STAGES) & 1, hdr, tmo, 0ull)) break;
+        if (*s_tile(s) >= ntiles) break;
+      } else {
+        have_next = reduce_pass(k + 1);
+      }
+      // scan pass of use k
+      if constexpr (Trace::kOn)
+        if (w == 0 && lane == 0) trace_now(kTrPWait, *s_tile(s));
       if (!mbar_wait_bounded(&prefb[s], (k / STAGES) & 1, hdr, tmo, 0ull)) break;
+      if constexpr (TK == 1)
+        if (w == 0 && lane == 0) ptx::mbar_arrive(&sgo[s]);
       const long long tile = *s_tile(s);
-      if (w == 0 && lane == 0) trace(kTrSStart, tile, ptx::globaltimer_ns());
+      if (w == 0 && lane == 0) trace_now(kTrSStart, tile);
       const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(tile, n, head);
       // exclusive prefix of this warp's segment inside the tile
       acc_t sx = (lane < w) ? s_aggs(s)[lane] : pol.aid();
       sx = warp_reduce(sx, aop, lane);
       const pre_t pw = pol.prepare(w == 0 ? *s_pref(s) : pol.cop(*s_pref(s), pol.to_carry(sx)));
+      if constexpr (LAY == 2) {
+        // rows: the row totals come from the reduce pass; one warp scan of
+        // them, then a thread-serial chain along the row
+        unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
+        const int r0 = w * Cfg::SEG + lane * (CH * V);
+        const bool interior = g.lo == 0 && g.blo == 0 && g.bhi == TILE;
+        const acc_t rt = s_rows(s)[w * 32 + lane];
+        const acc_t inc = warp_inclusive_scan(rt, aop, lane);
+        acc_t ex = shfl_up(inc, 1);
+        if (lane == 0) ex = pol.aid();
+        typename Pol::row_t row = pol.row_start(pol.extend(pw, ex));
+        auto chain = [&](auto excl_c) {
+#pragma unroll
+          for (int c = 0; c < CH; ++c) {
+            in_t x[V];
+            load_raw_at(s, r0 + c * V, g, interior, x);
+            union {
+              uint4 u;
+              out_t x[V];
+            } o;
+#pragma unroll
+            for (int j = 0; j < V; ++j) o.x[j] = decltype(excl_c)::value ? pol.row_excl(row, x[j]) : pol.row_incl(row, x[j]);
+            *reinterpret_cast<uint4*>(stage + size_t(r0 + c * V) * sizeof(in_t)) = o.u;
+          }
+        };
+        if (excl_kind)
+          chain(std::true_type{});
+        else
+          chain(std::false_type{});
+        __syncwarp();
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+          const int e0 = w * Cfg::SEG + (c * 32 + lane) * V;
+          union {
+            uint4 u;
+            out_t x[V];
+          } o;
+          o.u = *reinterpret_cast<const uint4*>(stage + size_t(e0) * sizeof(in_t));
+          if (out_vec && e0 >= g.lo && e0 + V <= g.valid) {
+            ptx::st_stream_v4(gout + (g.gbase + e0), o.u);
+          } else {
+#pragma unroll
+            for (int j = 0; j < V; ++j)
+              if (e0 + j >= g.lo && e0 + j < g.valid) gout[g.gbase + e0 + j] = o.x[j];
+          }
+        }
+      } else if constexpr (LAY == 1) {
+        // lane-blocked: this lane's row of CH chunks, one warp scan of the row
+        // totals, results written back in place, then streamed out striped
+        unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
+        const int r0 = w * Cfg::SEG + lane * (CH * V);
+        const bool interior = g.lo == 0 && g.blo == 0 && g.bhi == TILE;
+        acc_t a[CH][V];
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+          if (interior) {
+            union {
+              uint4 u;
+              in_t x[V];
+            } buf;
+            buf.u = *reinterpret_cast<const uint4*>(stage + size_t(r0 + c * V) * sizeof(in_t));
+#pragma unroll
+            for (int j = 0; j < V; ++j) a[c][j] = pol.load(buf.x[j]);
+          } else {
+            load_at(s, r0 + c * V, g, a[c]);
+          }
+#pragma unroll
+          for (int j = 1; j < V; ++j) a[c][j] = pol.aop(a[c][j - 1], a[c][j]);
+        }
+        // row prefix before each chunk (kept for small accumulators only)
+        constexpr bool kKeep = sizeof(acc_t) * CH <= 72;
+        acc_t P[kKeep ? CH : 1];
+        acc_t run = a[0][V - 1];
+#pragma unroll
+        for (int c = 1; c < CH; ++c) {
+          if constexpr (kKeep) P[c] = run;
+          run = pol.aop(run, a[c][V - 1]);
+        }
+        const acc_t inc = warp_inclusive_scan(run, aop, lane);
+        acc_t ex = shfl_up(inc, 1);
+        if (lane == 0) ex = pol.aid();
+        const pre_t pl = pol.extend(pw, ex);
+        pre_t cur = pl;
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+          pre_t pc;
+          if constexpr (kKeep) {
+            pc = c == 0 ? pl : pol.extend(pl, P[c]);
+          } else {
+            pc = cur;
+            if (c + 1 < CH) cur = pol.extend(cur, a[c][V - 1]);
+          }
+          union {
+            uint4 u;
+            out_t x[V];
+          } o;
+          TileScan<Pol, NC, CH, V>::finish_chunk(pol, pc, a[c], excl_kind, o.x);
+          *reinterpret_cast<uint4*>(stage + size_t(r0 + c * V) * sizeof(in_t)) = o.u;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+          const int e0 = w * Cfg::SEG + (c * 32 + lane) * V;
+          union {
+            uint4 u;
+            out_t x[V];
+          } o;
+          o.u = *reinterpret_cast<const uint4*>(stage + size_t(e0) * sizeof(in_t));
+          if (out_vec && e0 >= g.lo && e0 + V <= g.valid) {
+            ptx::st_stream_v4(gout + (g.gbase + e0), o.u);
+          } else {
+#pragma unroll
+            for (int j = 0; j < V; ++j)
+              if (e0 + j >= g.lo && e0 + j < g.valid) gout[g.gbase + e0 + j] = o.x[j];
+          }
+        }
+      } else {
       acc_t X = pol.aid();
       // chunks in groups of SG: the SG warp scans of a group are independent
       // and interleave, hiding shuffle and arithmetic latency
@@ -607,7 +974,7 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
         acc_t inc[SG];
 #pragma unroll
         for (int q = 0; q < SG; ++q) {
-          load_chunk(s, c0 + q, g, a[q]);
+          load_chunk(s, w, c0 + q, g, a[q]);
 #pragma unroll
           for (int j = 1; j < V; ++j) a[q][j] = pol.aop(a[q][j - 1], a[q][j]);
           inc[q] = a[q][V - 1];
@@ -636,9 +1003,10 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) decoupled_staged_kernel(cons
           }
         }
       }
+      }
       __syncwarp();
       if (lane == 0) {
-        if (w == 0) trace(kTrSDone, tile, ptx::globaltimer_ns());
+        if (w == 0) trace_now(kTrSDone, tile);
         ptx::mbar_arrive(&empty[s]);
       }
       have = have_next;

@@ -212,18 +212,50 @@ inline Status prepare_kernel(K kernel, int threads, size_t smem, int& blocks_per
 
 // ---------------------------------------------------------------------------
 // Decoupled look-back scan.
+// Policy classes of the tuning table.
+enum class TuneKind { int4, float4, wide8, compensated, fp64_carry };
+template <class Pol>
+struct tune_kind {
+  static constexpr TuneKind value = TuneKind::int4;
+};
+template <class T, class Op>
+struct tune_kind<PlainScan<T, Op>> {
+  static constexpr TuneKind value =
+      sizeof(T) == 8 ? TuneKind::wide8 : (std::is_same_v<T, float> ? TuneKind::float4 : TuneKind::int4);
+};
+template <>
+struct tune_kind<CompensatedF32> {
+  static constexpr TuneKind value = TuneKind::compensated;
+};
+template <>
+struct tune_kind<F64CarryF32> {
+  static constexpr TuneKind value = TuneKind::fp64_carry;
+};
+
+// Staged-kernel configuration per policy class, from sweeps of 2^32-byte
+// inputs on GB300 (all: 3 stages, one CTA per SM):
+//   int4         striped 64 KB tiles, ticket one stage life ahead;
+//   float4       rows of 9 chunks (72 KB tiles), late ticket, two polls;
+//   wide8        lane-blocked rows of 9 chunks (72 KB), late ticket, two polls;
+//   compensated  rows of 7 chunks over 20 warps (70 KB), late ticket, two polls;
+//   fp64_carry   as float4.
 template <class Pol>
 struct DecoupledTuning {
-  static constexpr int NC = 16;     // compute warps
-  static constexpr int CH = 8;      // 16-byte chunks per lane per segment (64 KB tiles)
+  static constexpr TuneKind K = tune_kind<Pol>::value;
+  static constexpr bool kRows = K == TuneKind::float4 || K == TuneKind::compensated || K == TuneKind::fp64_carry;
+  static constexpr int NC = K == TuneKind::compensated ? 20 : 16;  // compute warps
+  static constexpr int CH = K == TuneKind::int4 ? 8 : (K == TuneKind::compensated ? 7 : 9);  // chunks per lane
   static constexpr int STAGES = 3;  // shared-memory ring depth
-  static constexpr int LBW = 4;     // look-back windows of 32 tiles per round trip
+  static constexpr int LBW = (K == TuneKind::float4 || K == TuneKind::fp64_carry) ? 2 : 4;  // windows per poll
+  static constexpr int LAY = kRows ? 2 : (K == TuneKind::wide8 ? 1 : 0);  // striped / blocked / rows
+  static constexpr int TK = K == TuneKind::int4 ? 0 : 2;                  // when tickets are drawn
+  static constexpr unsigned PG = K == TuneKind::int4 ? 0u : 250u;         // second poll delay (ns)
   static constexpr int GEN_NC = 8;
   static constexpr int GEN_IPT = 8;
 };
 template <class Pol>
 using StagedFor = StagedCfg<Pol, DecoupledTuning<Pol>::NC, DecoupledTuning<Pol>::CH, DecoupledTuning<Pol>::STAGES,
-                            DecoupledTuning<Pol>::LBW>;
+                            DecoupledTuning<Pol>::LBW, DecoupledTuning<Pol>::LAY>;
 
 // The staged (bulk-copy) kernel takes any naturally aligned pointers of an
 // element type whose size divides 16 bytes; the tile grid is shifted so that
@@ -298,7 +330,7 @@ inline Status decoupled_scan(cudaStream_t s, const void* in, void* out, uint64_t
   if constexpr (16 % sizeof(typename Pol::in_t) == 0) {
     if (tma_path_ok<Pol>(in, out)) {
       using Cfg = StagedFor<Pol>;
-      auto k = decoupled_staged_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW>;
+      auto k = decoupled_staged_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Tn::LAY, Tn::TK, 0, Tn::PG>;
       int bps = 0;
       st = prepare_kernel(k, Cfg::THREADS, Cfg::SMEM, bps);
       if (st != Status::ok) return st;

@@ -5,6 +5,9 @@
 //   acc_t    in-tile accumulator (thread / warp / block scans)
 //   carry_t  tile aggregate and look-back carry (descriptor payload)
 //   pre_t    per-thread prepared carry used to finish outputs
+//   row_t    running state of a thread-serial scan along a row of elements
+//            (row_start from a prepared carry, then row_incl / row_excl per
+//            element, returning the output)
 //
 // PlainScan is the reference's semantics (one type, one operator).
 // CompensatedF32 keeps float-float (hi, lo) pairs everywhere: TwoSum
@@ -38,6 +41,19 @@ struct PlainScan {
   __device__ __forceinline__ pre_t extend(const pre_t& p, const acc_t& a) const { return op(p, a); }
   __device__ __forceinline__ out_t finish(const pre_t& p, const acc_t& a) const { return op(p, a); }
   __device__ __forceinline__ out_t finish_first(const pre_t& p) const { return p; }
+  __device__ __forceinline__ acc_t aop_in(const acc_t& a, const in_t& x) const { return op(a, x); }
+  __device__ __forceinline__ in_t in_id() const { return identity<Op, T>(); }
+  using row_t = T;
+  __device__ __forceinline__ row_t row_start(const pre_t& p) const { return p; }
+  __device__ __forceinline__ out_t row_incl(row_t& r, const in_t& x) const {
+    r = op(r, x);
+    return r;
+  }
+  __device__ __forceinline__ out_t row_excl(row_t& r, const in_t& x) const {
+    const out_t o = r;
+    r = op(r, x);
+    return o;
+  }
 };
 
 // float-float pair: value = hi + lo, |lo| <= ulp(hi)/2.
@@ -113,6 +129,26 @@ struct CompensatedF32 {
     return __fadd_rn(s, __fadd_rn(e, __fadd_rn(p.lo, a.lo)));
   }
   __device__ __forceinline__ out_t finish_first(const pre_t& p) const { return __fadd_rn(p.hi, p.lo); }
+  __device__ __forceinline__ in_t in_id() const { return 0.0f; }
+  // pair + element: TwoSum of the high parts, the error joins lo (lazily)
+  __device__ __forceinline__ acc_t aop_in(const acc_t& a, float x) const {
+    float s, e;
+    two_sum(a.hi, x, s, e);
+    return ff32{s, __fadd_rn(a.lo, e)};
+  }
+  // The running prefix is a lazy pair: every element is added with TwoSum,
+  // the output is the pair rounded to FP32.
+  using row_t = ff32;
+  __device__ __forceinline__ row_t row_start(const pre_t& p) const { return p; }
+  __device__ __forceinline__ out_t row_incl(row_t& r, float x) const {
+    r = aop_in(r, x);
+    return __fadd_rn(r.hi, r.lo);
+  }
+  __device__ __forceinline__ out_t row_excl(row_t& r, float x) const {
+    const float o = __fadd_rn(r.hi, r.lo);
+    r = aop_in(r, x);
+    return o;
+  }
 };
 
 struct F64CarryF32 {
@@ -137,6 +173,23 @@ struct F64CarryF32 {
     return __fadd_rn(p.hi, __fadd_rn(p.lo, a));
   }
   __device__ __forceinline__ out_t finish_first(const pre_t& p) const { return __fadd_rn(p.hi, p.lo); }
+  __device__ __forceinline__ acc_t aop_in(float a, float x) const { return __fadd_rn(a, x); }
+  __device__ __forceinline__ in_t in_id() const { return 0.0f; }
+  // FP32 running sum inside the row, added to the prepared carry per output
+  struct row_t {
+    ff32 p;
+    float a;
+  };
+  __device__ __forceinline__ row_t row_start(const pre_t& p) const { return row_t{p, 0.0f}; }
+  __device__ __forceinline__ out_t row_incl(row_t& r, float x) const {
+    r.a = __fadd_rn(r.a, x);
+    return finish(r.p, r.a);
+  }
+  __device__ __forceinline__ out_t row_excl(row_t& r, float x) const {
+    const float o = finish(r.p, r.a);
+    r.a = __fadd_rn(r.a, x);
+    return o;
+  }
 };
 
 }  // namespace pp

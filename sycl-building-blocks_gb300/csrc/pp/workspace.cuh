@@ -87,16 +87,26 @@ struct desc_codec {
     }
   }
 
-  // Returns the status of descriptor `d` in epoch tag `etag` (= epoch+1) and
-  // its payload in `v`; kInvalid when not (fully) written in this epoch.
-  __device__ __forceinline__ static uint32_t read(const uint64_t* d, uint32_t etag, C& v) {
-    uint64_t w[W];
+  // Issues the loads of descriptor `d` (decode() consumes them later, so
+  // several polls can be in flight).
+  __device__ __forceinline__ static void load_raw(const uint64_t* d, uint64_t (&w)[W]) {
     if constexpr (W == 1) {
       w[0] = ptx::ld_relaxed(d);
     } else {
 #pragma unroll
       for (int i = 0; i < W; i += 2) ptx::ld_relaxed_v2(d + i, w[i], w[i + 1]);
     }
+  }
+
+  // Returns the status of descriptor `d` in epoch tag `etag` (= epoch+1) and
+  // its payload in `v`; kInvalid when not (fully) written in this epoch.
+  __device__ __forceinline__ static uint32_t read(const uint64_t* d, uint32_t etag, C& v) {
+    uint64_t w[W];
+    load_raw(d, w);
+    return decode(w, etag, v);
+  }
+
+  __device__ __forceinline__ static uint32_t decode(const uint64_t (&w)[W], uint32_t etag, C& v) {
     const uint32_t tag = uint32_t(w[0] >> 32);
     bool same = true;
 #pragma unroll
