@@ -88,6 +88,26 @@ Status reduce_dispatch(cudaStream_t s, pp_op op, pp_dtype dt, const void* in, ui
   return Status::invalid_arg;
 }
 
+Status dispatch_carry(pp_dtype dt, cudaStream_t s, pp_op op, void* out, const void* in, uint64_t n,
+                      const void* carry_prev, void* carry_next, bool excl, bool first) {
+  using namespace pp::capi;
+  switch (dt) {
+    case PP_I32:
+      return carry_typed<int32_t>(s, op, out, in, n, carry_prev, carry_next, excl, first);
+    case PP_U32:
+      return carry_typed<uint32_t>(s, op, out, in, n, carry_prev, carry_next, excl, first);
+    case PP_I64:
+      return carry_typed<int64_t>(s, op, out, in, n, carry_prev, carry_next, excl, first);
+    case PP_U64:
+      return carry_typed<uint64_t>(s, op, out, in, n, carry_prev, carry_next, excl, first);
+    case PP_F32:
+      return carry_typed<float>(s, op, out, in, n, carry_prev, carry_next, excl, first);
+    case PP_F64:
+      return carry_typed<double>(s, op, out, in, n, carry_prev, carry_next, excl, first);
+  }
+  return Status::invalid_arg;
+}
+
 pp_status scan_entry(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dt, const void* in, void* out,
                      uint64_t n, pp_scan_algo algo, pp_precision prec, void* ws, size_t ws_bytes) {
   pp_status c = check_scan_args(kind, op, dt, in, out, n, algo, prec);
@@ -106,35 +126,50 @@ pp_status scan_entry(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dt,
   return to_c(scan_dispatch(r, dt, prec));
 }
 
-// Device buffers reused by the blocking host-pointer wrappers.
-struct HostStaging {
+// Host-pointer scans stream the array through the GPU in chunks on three
+// streams: copy in (chunk i+1), scan and offset (chunk i), copy out (chunk
+// i-1) overlap, and the copy engines run both directions at once. Chunk i is
+// scanned on its own and offset by the running total of chunks 0..i-1 (kept
+// on the device, double-buffered). A ring of kSlots chunk buffers bounds the
+// device memory at 2 * kSlots * kChunkBytes.
+constexpr size_t kChunkBytes = size_t(64) << 20;
+constexpr int kSlots = 4;
+constexpr uint64_t kMaxChunks = 16384;  // per-chunk partial results of a host reduction (1 TiB of input)
+
+struct HostPipeline {
   std::mutex mu;
-  void* d_in = nullptr;
-  void* d_out = nullptr;
-  size_t bytes = 0;
   int device = -1;
+  cudaStream_t h2d = nullptr, comp = nullptr, d2h = nullptr;
+  cudaEvent_t in_ready[kSlots] = {}, out_ready[kSlots] = {}, slot_free[kSlots] = {};
+  void* d_in[kSlots] = {};
+  void* d_out[kSlots] = {};
+  void* carry = nullptr;     // two 16-byte running totals
+  void* result = nullptr;    // one reduction result
+  void* partials = nullptr;  // kMaxChunks per-chunk reduction results
 };
-HostStaging& staging() {
-  static HostStaging* s = new HostStaging();
-  return *s;
+HostPipeline& pipeline() {
+  static HostPipeline* p = new HostPipeline();
+  return *p;
 }
 
-pp_status ensure_staging(HostStaging& st, size_t bytes) {
+pp_status ensure_pipeline(HostPipeline& p) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return PP_ERR_NO_DEVICE;
-  if (st.device == dev && st.bytes >= bytes) return PP_OK;
-  if (st.d_in) cudaFree(st.d_in);
-  if (st.d_out) cudaFree(st.d_out);
-  st.d_in = st.d_out = nullptr;
-  st.bytes = 0;
-  if (cudaMalloc(&st.d_in, bytes) != cudaSuccess) return PP_ERR_CUDA;
-  if (cudaMalloc(&st.d_out, bytes) != cudaSuccess) {
-    cudaFree(st.d_in);
-    st.d_in = nullptr;
-    return PP_ERR_CUDA;
+  if (p.device == dev) return PP_OK;
+  if (p.device >= 0) return PP_ERR_UNSUPPORTED;  // one device per process for the host entry points
+  bool ok = cudaStreamCreateWithFlags(&p.h2d, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&p.comp, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&p.d2h, cudaStreamNonBlocking) == cudaSuccess;
+  for (int k = 0; ok && k < kSlots; ++k) {
+    ok = cudaEventCreateWithFlags(&p.in_ready[k], cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&p.out_ready[k], cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&p.slot_free[k], cudaEventDisableTiming) == cudaSuccess &&
+         cudaMalloc(&p.d_in[k], kChunkBytes) == cudaSuccess && cudaMalloc(&p.d_out[k], kChunkBytes) == cudaSuccess;
   }
-  st.bytes = bytes;
-  st.device = dev;
+  ok = ok && cudaMalloc(&p.carry, 32) == cudaSuccess && cudaMalloc(&p.result, 16) == cudaSuccess &&
+       cudaMalloc(&p.partials, kMaxChunks * 8) == cudaSuccess;
+  if (!ok) return PP_ERR_CUDA;
+  p.device = dev;
   return PP_OK;
 }
 
@@ -143,17 +178,48 @@ pp_status host_scan_entry(pp_scan_kind kind, pp_op op, pp_dtype dt, const void* 
   pp_status c = check_scan_args(kind, op, dt, h_in, h_out, n, algo, PP_PREC_DEFAULT);
   if (c != PP_OK) return c;
   if (n == 0) return PP_OK;
-  const size_t bytes = n * dtype_size(dt);
-  HostStaging& st = staging();
-  std::lock_guard<std::mutex> g(st.mu);
-  c = ensure_staging(st, bytes);
+  const size_t esz = dtype_size(dt);
+  const uint64_t chunk = kChunkBytes / esz;
+  const uint64_t chunks = (n + chunk - 1) / chunk;
+  HostPipeline& p = pipeline();
+  std::lock_guard<std::mutex> g(p.mu);
+  c = ensure_pipeline(p);
   if (c != PP_OK) return c;
-  cudaStream_t s = nullptr;
-  if (cudaMemcpyAsync(st.d_in, h_in, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return PP_ERR_CUDA;
-  c = scan_entry(s, kind, op, dt, st.d_in, st.d_out, n, algo, PP_PREC_DEFAULT, nullptr, 0);
+  const bool excl = kind == PP_SCAN_EXCLUSIVE;
+  const unsigned char* hi = static_cast<const unsigned char*>(h_in);
+  unsigned char* ho = static_cast<unsigned char*>(h_out);
+  unsigned char* carry = static_cast<unsigned char*>(p.carry);
+  for (uint64_t i = 0; i < chunks && c == PP_OK; ++i) {
+    const int k = int(i % kSlots);
+    const uint64_t off = i * chunk;
+    const uint64_t m = n - off < chunk ? n - off : chunk;
+    const size_t bytes = m * esz;
+    // the slot's previous chunk must be out before its buffers are reused
+    if (i >= uint64_t(kSlots) && cudaStreamWaitEvent(p.h2d, p.slot_free[k], 0) != cudaSuccess) c = PP_ERR_CUDA;
+    if (c == PP_OK && cudaMemcpyAsync(p.d_in[k], hi + off * esz, bytes, cudaMemcpyHostToDevice, p.h2d) != cudaSuccess)
+      c = PP_ERR_CUDA;
+    if (c == PP_OK && (cudaEventRecord(p.in_ready[k], p.h2d) != cudaSuccess ||
+                       cudaStreamWaitEvent(p.comp, p.in_ready[k], 0) != cudaSuccess))
+      c = PP_ERR_CUDA;
+    if (c == PP_OK) c = scan_entry(p.comp, kind, op, dt, p.d_in[k], p.d_out[k], m, algo, PP_PREC_DEFAULT, nullptr, 0);
+    if (c == PP_OK) {
+      c = to_c(dispatch_carry(dt, p.comp, op, p.d_out[k], p.d_in[k], m, carry + ((i + 1) & 1) * 16,
+                              carry + (i & 1) * 16, excl, i == 0));
+    }
+    if (c == PP_OK && (cudaEventRecord(p.out_ready[k], p.comp) != cudaSuccess ||
+                       cudaStreamWaitEvent(p.d2h, p.out_ready[k], 0) != cudaSuccess))
+      c = PP_ERR_CUDA;
+    if (c == PP_OK && cudaMemcpyAsync(ho + off * esz, p.d_out[k], bytes, cudaMemcpyDeviceToHost, p.d2h) != cudaSuccess)
+      c = PP_ERR_CUDA;
+    if (c == PP_OK && cudaEventRecord(p.slot_free[k], p.d2h) != cudaSuccess) c = PP_ERR_CUDA;
+  }
+  // nothing may still read or write the caller's buffers when this returns
+  const cudaError_t e1 = cudaStreamSynchronize(p.h2d);
+  const cudaError_t e2 = cudaStreamSynchronize(p.comp);
+  const cudaError_t e3 = cudaStreamSynchronize(p.d2h);
   if (c != PP_OK) return c;
-  if (cudaMemcpyAsync(h_out, st.d_out, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess) return PP_ERR_CUDA;
-  return to_c(pp::host::read_device_error(s, nullptr));
+  if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) return PP_ERR_CUDA;
+  return to_c(pp::host::read_device_error(p.comp, nullptr));
 }
 
 }  // namespace
@@ -251,13 +317,13 @@ pp_status pp_reduce_device(pp_stream stream, pp_op op, pp_dtype dtype, const voi
   if (n > 0 && !aligned_to(d_in, dtype_size(dtype))) return PP_ERR_INVALID_ARG;
   if (is_float(dtype) && is_bitop(op)) return PP_ERR_UNSUPPORTED;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  HostStaging& st = staging();
-  std::lock_guard<std::mutex> g(st.mu);
-  pp_status c = ensure_staging(st, 16);
+  HostPipeline& p = pipeline();
+  std::lock_guard<std::mutex> g(p.mu);
+  pp_status c = ensure_pipeline(p);
   if (c != PP_OK) return c;
-  Status r = reduce_dispatch(s, op, dtype, d_in, n, st.d_out, nullptr, 0);
+  Status r = reduce_dispatch(s, op, dtype, d_in, n, p.result, nullptr, 0);
   if (r != Status::ok) return to_c(r);
-  if (cudaMemcpyAsync(h_result, st.d_out, dtype_size(dtype), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+  if (cudaMemcpyAsync(h_result, p.result, dtype_size(dtype), cudaMemcpyDeviceToHost, s) != cudaSuccess)
     return PP_ERR_CUDA;
   return to_c(pp::host::read_device_error(s, nullptr));
 }
@@ -277,18 +343,39 @@ pp_status pp_scan_host(pp_scan_kind kind, pp_op op, pp_dtype dtype, const void* 
 pp_status pp_reduce_host(pp_op op, pp_dtype dtype, const void* h_in, uint64_t n, void* h_result) {
   if (!h_result || !valid_op(op) || !valid_dtype(dtype) || (n > 0 && !h_in)) return PP_ERR_INVALID_ARG;
   if (is_float(dtype) && is_bitop(op)) return PP_ERR_UNSUPPORTED;
-  const size_t bytes = n * dtype_size(dtype);
-  HostStaging& st = staging();
-  std::lock_guard<std::mutex> g(st.mu);
-  pp_status c = ensure_staging(st, bytes < 16 ? 16 : bytes);
+  const size_t esz = dtype_size(dtype);
+  const uint64_t chunk = kChunkBytes / esz;
+  const uint64_t chunks = (n + chunk - 1) / chunk;
+  if (chunks > kMaxChunks) return PP_ERR_UNSUPPORTED;
+  HostPipeline& p = pipeline();
+  std::lock_guard<std::mutex> g(p.mu);
+  pp_status c = ensure_pipeline(p);
   if (c != PP_OK) return c;
-  cudaStream_t s = nullptr;
-  if (bytes && cudaMemcpyAsync(st.d_in, h_in, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return PP_ERR_CUDA;
-  Status r = reduce_dispatch(s, op, dtype, st.d_in, n, st.d_out, nullptr, 0);
-  if (r != Status::ok) return to_c(r);
-  if (cudaMemcpyAsync(h_result, st.d_out, dtype_size(dtype), cudaMemcpyDeviceToHost, s) != cudaSuccess)
-    return PP_ERR_CUDA;
-  return to_c(pp::host::read_device_error(s, nullptr));
+  // every chunk is reduced on its own while the next one streams in; the
+  // per-chunk results are reduced last
+  const unsigned char* hi = static_cast<const unsigned char*>(h_in);
+  unsigned char* parts = static_cast<unsigned char*>(p.partials);
+  for (uint64_t i = 0; i < chunks && c == PP_OK; ++i) {
+    const int k = int(i % kSlots);
+    const uint64_t off = i * chunk;
+    const uint64_t m = n - off < chunk ? n - off : chunk;
+    if (i >= uint64_t(kSlots) && cudaStreamWaitEvent(p.h2d, p.slot_free[k], 0) != cudaSuccess) c = PP_ERR_CUDA;
+    if (c == PP_OK && cudaMemcpyAsync(p.d_in[k], hi + off * esz, m * esz, cudaMemcpyHostToDevice, p.h2d) != cudaSuccess)
+      c = PP_ERR_CUDA;
+    if (c == PP_OK && (cudaEventRecord(p.in_ready[k], p.h2d) != cudaSuccess ||
+                       cudaStreamWaitEvent(p.comp, p.in_ready[k], 0) != cudaSuccess))
+      c = PP_ERR_CUDA;
+    if (c == PP_OK) c = to_c(reduce_dispatch(p.comp, op, dtype, p.d_in[k], m, parts + i * esz, nullptr, 0));
+    if (c == PP_OK && cudaEventRecord(p.slot_free[k], p.comp) != cudaSuccess) c = PP_ERR_CUDA;
+  }
+  if (c == PP_OK) c = to_c(reduce_dispatch(p.comp, op, dtype, parts, chunks, p.result, nullptr, 0));
+  if (c == PP_OK && cudaMemcpyAsync(h_result, p.result, esz, cudaMemcpyDeviceToHost, p.comp) != cudaSuccess)
+    c = PP_ERR_CUDA;
+  const cudaError_t e1 = cudaStreamSynchronize(p.h2d);
+  const cudaError_t e2 = cudaStreamSynchronize(p.comp);
+  if (c != PP_OK) return c;
+  if (e1 != cudaSuccess || e2 != cudaSuccess) return PP_ERR_CUDA;
+  return to_c(pp::host::read_device_error(p.comp, nullptr));
 }
 
 const char* pp_status_string(pp_status status) {

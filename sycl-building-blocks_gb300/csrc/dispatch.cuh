@@ -36,6 +36,11 @@ Status reduce_typed(cudaStream_t s, pp_op op, const void* in, uint64_t n, void* 
                     size_t ws_bytes);
 template <class T>
 size_t workspace_typed(pp_scan_algo algo, const void* in, const void* out, uint64_t n);
+// Offsets chunk `out` (n elements, scanned on its own) by *carry_prev and
+// records the running total in *carry_next; the first chunk only records.
+template <class T>
+Status carry_typed(cudaStream_t s, pp_op op, void* out, const void* in, uint64_t n, const void* carry_prev,
+                   void* carry_next, bool exclusive, bool first);
 
 // Batched segmented scan / reduce and row scans (capi_seg_<type>.cu).
 struct SegReq {

@@ -4,6 +4,7 @@
 #include <type_traits>
 
 #include "dispatch.cuh"
+#include "pp/carry.cuh"
 
 namespace pp {
 namespace capi {
@@ -86,6 +87,54 @@ size_t workspace_typed(pp_scan_algo algo, const void* in, const void* out, uint6
   return workspace_policy<PlainScan<T, plus>>(algo, in, out, n);
 }
 
+template <class T, class Op>
+Status carry_op(cudaStream_t s, void* out, const void* in, uint64_t n, const void* carry_prev, void* carry_next,
+                bool exclusive, bool first) {
+  if (n == 0) return Status::ok;
+  T* o = static_cast<T*>(out);
+  const T* i = static_cast<const T*>(in);
+  if (first) {
+    carry_first_kernel<T, Op><<<1, 32, 0, s>>>(o, i, n, static_cast<T*>(carry_next), exclusive ? 1 : 0);
+  } else {
+    host::DeviceInfo di;
+    const Status st = host::device_info(di);
+    if (st != Status::ok) return st;
+    const uint64_t vecs = n / (16 / sizeof(T));
+    uint64_t grid = (vecs + 255) / 256;
+    if (grid > uint64_t(di.sm_count) * 8) grid = uint64_t(di.sm_count) * 8;
+    if (grid == 0) grid = 1;
+    carry_apply_kernel<T, Op><<<unsigned(grid), 256, 0, s>>>(o, i, n, static_cast<const T*>(carry_prev),
+                                                            static_cast<T*>(carry_next), exclusive ? 1 : 0);
+  }
+  return host::from_cuda(cudaGetLastError());
+}
+
+template <class T>
+Status carry_typed(cudaStream_t s, pp_op op, void* out, const void* in, uint64_t n, const void* carry_prev,
+                   void* carry_next, bool exclusive, bool first) {
+  switch (op) {
+    case PP_OP_PLUS:
+      return carry_op<T, plus>(s, out, in, n, carry_prev, carry_next, exclusive, first);
+    case PP_OP_MULTIPLIES:
+      return carry_op<T, multiplies>(s, out, in, n, carry_prev, carry_next, exclusive, first);
+    case PP_OP_MINIMUM:
+      return carry_op<T, minimum>(s, out, in, n, carry_prev, carry_next, exclusive, first);
+    case PP_OP_MAXIMUM:
+      return carry_op<T, maximum>(s, out, in, n, carry_prev, carry_next, exclusive, first);
+    case PP_OP_BIT_AND:
+    case PP_OP_BIT_OR:
+    case PP_OP_BIT_XOR:
+      if constexpr (std::is_integral_v<T>) {
+        if (op == PP_OP_BIT_AND) return carry_op<T, bit_and>(s, out, in, n, carry_prev, carry_next, exclusive, first);
+        if (op == PP_OP_BIT_OR) return carry_op<T, bit_or>(s, out, in, n, carry_prev, carry_next, exclusive, first);
+        return carry_op<T, bit_xor>(s, out, in, n, carry_prev, carry_next, exclusive, first);
+      } else {
+        return Status::unsupported;
+      }
+  }
+  return Status::invalid_arg;
+}
+
 // Segmented operators: plus, minimum, maximum.
 template <class T, class F>
 Status with_seg_op(pp_op op, F&& f) {
@@ -136,7 +185,8 @@ Status rows_scan_typed(const SegReq& r) {
 #define PP_INSTANTIATE_DISPATCH(T)                                                                     \
   template Status scan_typed<T>(const ScanReq&);                                                       \
   template Status reduce_typed<T>(cudaStream_t, pp_op, const void*, uint64_t, void*, void*, size_t); \
-  template size_t workspace_typed<T>(pp_scan_algo, const void*, const void*, uint64_t);
+  template size_t workspace_typed<T>(pp_scan_algo, const void*, const void*, uint64_t);                \
+  template Status carry_typed<T>(cudaStream_t, pp_op, void*, const void*, uint64_t, const void*, void*, bool, bool);
 
 }  // namespace capi
 }  // namespace pp

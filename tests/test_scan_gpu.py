@@ -195,6 +195,28 @@ def test_host_wrappers(pp, oracle, cuda):
     np.testing.assert_array_equal(pp.scan_host("inclusive", "maximum", x), oracle.scan(x, "maximum"))
 
 
+@pytest.mark.parametrize("dtype,op,excl", [("u32", "plus", False), ("i32", "maximum", True), ("u64", "bit_xor", True),
+                                           ("f64", "minimum", False)])
+def test_host_wrappers_stream_several_chunks(pp, oracle, cuda, dtype, op, excl):
+    """Host arrays larger than one 64 MiB chunk: chunks are scanned on their
+    own and offset by the running total of the chunks before them."""
+    esz = 8 if dtype in ("u64", "f64") else 4
+    n = 2 * (64 << 20) // esz + 12345  # two full chunks and a ragged third
+    x = make_input(dtype, op, n, seed=21)
+    kind = "exclusive" if excl else "inclusive"
+    np.testing.assert_array_equal(pp.decoupled_scan(kind, op, x), oracle.scan(x, op, excl))
+    if dtype == "u32":
+        np.testing.assert_array_equal(pp.cooperative_scan(kind, op, x), oracle.scan(x, op, excl))
+
+
+def test_host_reduce_streams_several_chunks(pp, oracle, cuda):
+    n = (64 << 20) // 8 * 3 + 7
+    x = make_input("u64", "plus", n, seed=22)
+    assert int(pp.reduce_host("plus", x)) == int(oracle.reduce(x, "plus"))
+    assert int(pp.reduce_host("maximum", x)) == int(x.max())
+    assert int(pp.reduce_host("plus", x[:0])) == 0
+
+
 def test_bad_arguments(pp, cuda):
     d = cuda.zeros(16, dtype=cuda.float32, device="cuda")
     with pytest.raises(pp.PPError) as e:
