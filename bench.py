@@ -573,6 +573,73 @@ def run_reference(args) -> dict | None:
     }
 
 
+def run_profile_cases(args) -> dict:
+    """One launch of every kernel of the path on inputs larger than L2 (a few
+    hundred MB each, about 3 GB in total), no timing: the command the ncu
+    captures in profiles/ run. Prints the case order."""
+    import torch
+
+    import ppbuild
+
+    ppbuild.build()
+    import ppgb300 as pp
+
+    pp.lib()
+    sh = torch.cuda.current_stream().cuda_stream
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    n = 1 << 26  # 256 MiB of 4-byte elements
+    u = torch.randint(0, 1 << 16, (n,), dtype=torch.int32, device="cuda", generator=g)
+    f = torch.randn(n, dtype=torch.float32, device="cuda", generator=g)
+    o = torch.empty_like(u)
+    w = torch.randint(0, 1 << 32, (n // 2,), dtype=torch.int64, device="cuda", generator=g)
+    ow = torch.empty_like(w)
+    res = torch.empty(4, dtype=torch.float64, device="cuda")
+    cases = []
+
+    def case(name, fn):
+        fn()
+        torch.cuda.synchronize()
+        if pp.stream_status(sh) != 0:
+            raise RuntimeError(f"device error in profile case {name}")
+        cases.append(name)
+
+    case("u32 inclusive plus 2^26", lambda: pp.decoupled_scan_device("inclusive", "plus", u.data_ptr(), o.data_ptr(),
+                                                                       n, "u32", stream=sh))
+    case("u32 exclusive plus 2^26", lambda: pp.decoupled_scan_device("exclusive", "plus", u.data_ptr(), o.data_ptr(),
+                                                                       n, "u32", stream=sh))
+    case("i32 inclusive maximum 2^26", lambda: pp.decoupled_scan_device("inclusive", "maximum", u.data_ptr(),
+                                                                          o.data_ptr(), n, "i32", stream=sh))
+    case("u64 inclusive plus 2^25", lambda: pp.decoupled_scan_device("inclusive", "plus", w.data_ptr(), ow.data_ptr(),
+                                                                       n // 2, "u64", stream=sh))
+    for prec in ("default", "compensated", "fp64_carry"):
+        case(f"f32 inclusive plus {prec} 2^26",
+             lambda p=prec: pp.scan("inclusive", "plus", f.data_ptr(), o.data_ptr(), n, "f32", stream=sh, precision=p))
+    case("u32 cooperative inclusive plus 2^26", lambda: pp.cooperative_scan_device("inclusive", "plus", u.data_ptr(),
+                                                                                   o.data_ptr(), n, "u32", stream=sh))
+    case("f32 sum reduce 2^26", lambda: pp.reduce("plus", f.data_ptr(), n, "f32", res.data_ptr(), stream=sh))
+    case("u64 sum reduce 2^25", lambda: pp.reduce("plus", w.data_ptr(), n // 2, "u64", res.data_ptr(), stream=sh))
+    segs = 16384
+    gc = torch.Generator(device="cpu").manual_seed(0x5EC)
+    lens = torch.floor(torch.exp(torch.rand(segs, generator=gc, dtype=torch.float64) * math.log(2 ** 13)))
+    offs = torch.zeros(segs + 1, dtype=torch.int64)
+    offs[1:] = torch.cumsum(lens.clamp(1, 2 ** 13).to(torch.int64), 0)
+    ns = int(offs[-1])
+    d_off = offs.cuda()
+    case(f"i32 segmented plus scan {segs} segments {ns} elements",
+         lambda: pp.segmented_scan("inclusive", "plus", u.data_ptr(), o.data_ptr(), ns, d_off.data_ptr(), segs, "i32",
+                                   stream=sh))
+    seg_out = torch.empty(segs, dtype=torch.int32, device="cuda")
+    case(f"i32 segmented plus reduce {segs} segments",
+         lambda: pp.segmented_reduce("plus", u.data_ptr(), ns, d_off.data_ptr(), segs, seg_out.data_ptr(), "i32",
+                                     stream=sh))
+    case("f32 row scans 8192 x 8192 forward", lambda: pp.rows_scan("inclusive", "plus", f.data_ptr(), o.data_ptr(),
+                                                                     8192, 8192, "f32", stream=sh))
+    case("f32 row scans 8192 x 8192 reverse", lambda: pp.rows_scan("inclusive", "plus", f.data_ptr(), o.data_ptr(),
+                                                                     8192, 8192, "f32", reverse=True, stream=sh))
+    case("device copy 256 MiB (torch, reference point)", lambda: o.copy_(u))
+    return {"profile_cases": cases}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -585,7 +652,12 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-cases", action="store_true",
+                    help="run each kernel of the path once on a small case (the ncu capture command)")
     args = ap.parse_args()
+    if args.profile_cases:
+        print(json.dumps(run_profile_cases(args)), flush=True)
+        return
     if args.warmup < 3:
         args.warmup = 3
     res = run_reference(args) if args.impl == "reference" else run_ours(args)

@@ -304,6 +304,30 @@ __device__ __forceinline__ StagedGeom staged_geom(long long t, uint64_t n, int h
   return g;
 }
 
+// V elements of a tile at offset e0 next to a ragged edge: bulk-copied ones
+// from the stage, the rest of the valid range from global memory, the
+// identity outside it.
+template <class T, int V>
+struct EdgeChunk {
+  T x[V];
+};
+template <class T, int V>
+__device__ __noinline__ EdgeChunk<T, V> load_edge_chunk(const unsigned char* stage, const T* gin, StagedGeom g,
+                                                         int e0, T id) {
+  EdgeChunk<T, V> c;
+#pragma unroll
+  for (int j = 0; j < V; ++j) {
+    const int e = e0 + j;
+    if (e < g.lo || e >= g.valid)
+      c.x[j] = id;
+    else if (e >= g.blo && e < g.bhi)
+      c.x[j] = reinterpret_cast<const T*>(stage)[e];
+    else
+      c.x[j] = gin[g.gbase + e];
+  }
+  return c;
+}
+
 // Warp-wide look-back reading LBW windows of 32 descriptors per round trip.
 template <class Pol, int LBW>
 __device__ __forceinline__ bool lookback_multi(const Pol& pol, const uint64_t* desc, long long tile,
@@ -509,6 +533,10 @@ __device__ __forceinline__ bool lookback_pipelined(const Pol& pol, const uint64_
 // they arrive (up to STAGES-1 ahead of the scan), so a late prefix never
 // delays the publication of the next aggregates.
 // PG: 0 = one look-back poll in flight; > 0 = two, the second PG ns later.
+// BS: 1 = in the row layouts each compute warp writes its finished segment
+// back with one bulk copy (shared -> global) instead of striped stores.
+// EXC: -1 = scan kind read from the arguments; 0 / 1 = inclusive / exclusive
+// compiled in (one code path: smaller kernels for the instruction cache).
 // TK: when the producer draws the ticket of the next tile for a stage.
 //   0: right after issuing the previous copy (a full stage life ahead);
 //   1: when the compute warps start scanning the tile still in that stage;
@@ -517,7 +545,7 @@ __device__ __forceinline__ bool lookback_pipelined(const Pol& pol, const uint64_
 // reach their reduce pass more closely, so predecessors' aggregates arrive
 // closer together; earlier ones hide the latency of the ticket atomic.
 template <class Pol, int NC, int CH, int STAGES, int LBW, int LAY = 0, int TK = 0, int NR = 0,
-          unsigned PG = 0, class Trace = NoTrace>
+          unsigned PG = 0, int EXC = -1, int BS = 0, class Trace = NoTrace>
 __global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel(const ScanArgs args) {
   using Cfg = StagedCfg<Pol, NC, CH, STAGES, LBW, LAY, NR>;
   using in_t = typename Pol::in_t;
@@ -671,7 +699,7 @@ __global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel
     const int w = NR > 0 ? (reducer ? warp - 2 : warp - 2 - NR) : warp - 2;
     const in_t* gin = static_cast<const in_t*>(args.in);
     out_t* gout = static_cast<out_t*>(args.out);
-    const bool excl_kind = args.exclusive != 0;
+    const bool excl_kind = EXC >= 0 ? EXC == 1 : args.exclusive != 0;
     auto aop = [&](const acc_t& x, const acc_t& y) { return pol.aop(x, y); };
 
     const bool out_vec = ((reinterpret_cast<uintptr_t>(gout) - uintptr_t(head) * sizeof(out_t)) & 15u) == 0;
@@ -700,6 +728,8 @@ __global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel
       }
     };
     // V raw elements at tile offset e0, the identity outside the valid range
+    // (the ragged edges of the array take an out-of-line path: it keeps the
+    // unrolled loops of interior tiles small)
     auto load_raw_at = [&](int s, int e0, const StagedGeom& g, bool interior, in_t (&x)[V]) {
       const unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
       if (interior || (e0 >= g.blo && e0 + V <= g.bhi)) {
@@ -711,21 +741,48 @@ __global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel
 #pragma unroll
         for (int j = 0; j < V; ++j) x[j] = buf.x[j];
       } else {
+        const EdgeChunk<in_t, V> c = load_edge_chunk<in_t, V>(stage, gin, g, e0, pol.in_id());
 #pragma unroll
-        for (int j = 0; j < V; ++j) {
-          const int e = e0 + j;
-          if (e < g.lo || e >= g.valid)
-            x[j] = pol.in_id();
-          else if (e >= g.blo && e < g.bhi)
-            x[j] = reinterpret_cast<const in_t*>(stage)[e];
-          else
-            x[j] = gin[g.gbase + e];
-        }
+        for (int j = 0; j < V; ++j) x[j] = c.x[j];
       }
     };
     // striped chunk c of this lane in segment seg: tile offset seg*SEG + (c*32 + lane)*V
     auto load_chunk = [&](int s, int seg, int c, const StagedGeom& g, acc_t (&a)[V]) {
       load_at(s, seg * Cfg::SEG + (c * 32 + lane) * V, g, a);
+    };
+    // Writes this warp's finished segment (already in the stage, in order):
+    // one bulk copy when the whole segment is valid and the output aligned,
+    // else striped 16-byte stores. Returns once the stage may be reused.
+    auto store_segment = [&](const unsigned char* stage, const StagedGeom& g) {
+      const int s0 = w * Cfg::SEG;
+      if (BS && out_vec && s0 >= g.lo && s0 + Cfg::SEG <= g.valid) {
+        ptx::fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) {
+          ptx::bulk_s2g_hint(gout + (g.gbase + s0), stage + size_t(s0) * sizeof(in_t),
+                             uint32_t(Cfg::SEG * sizeof(out_t)), ptx::policy_evict_first());
+          ptx::bulk_commit();
+          ptx::bulk_wait_read<0>();
+        }
+        return;
+      }
+      __syncwarp();
+#pragma unroll
+      for (int c = 0; c < CH; ++c) {
+        const int e0 = s0 + (c * 32 + lane) * V;
+        union {
+          uint4 u;
+          out_t x[V];
+        } o;
+        o.u = *reinterpret_cast<const uint4*>(stage + size_t(e0) * sizeof(in_t));
+        if (out_vec && e0 >= g.lo && e0 + V <= g.valid) {
+          ptx::st_stream_v4(gout + (g.gbase + e0), o.u);
+        } else {
+#pragma unroll
+          for (int j = 0; j < V; ++j)
+            if (e0 + j >= g.lo && e0 + j < g.valid) gout[g.gbase + e0 + j] = o.x[j];
+        }
+      }
     };
     // aggregate of segment seg of stage s (a warp-wide value)
     auto reduce_segment = [&](int s, int seg, const StagedGeom& g) -> acc_t {
@@ -872,27 +929,17 @@ __global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel
             *reinterpret_cast<uint4*>(stage + size_t(r0 + c * V) * sizeof(in_t)) = o.u;
           }
         };
-        if (excl_kind)
+        if constexpr (EXC == 1) {
           chain(std::true_type{});
-        else
+        } else if constexpr (EXC == 0) {
           chain(std::false_type{});
-        __syncwarp();
-#pragma unroll
-        for (int c = 0; c < CH; ++c) {
-          const int e0 = w * Cfg::SEG + (c * 32 + lane) * V;
-          union {
-            uint4 u;
-            out_t x[V];
-          } o;
-          o.u = *reinterpret_cast<const uint4*>(stage + size_t(e0) * sizeof(in_t));
-          if (out_vec && e0 >= g.lo && e0 + V <= g.valid) {
-            ptx::st_stream_v4(gout + (g.gbase + e0), o.u);
-          } else {
-#pragma unroll
-            for (int j = 0; j < V; ++j)
-              if (e0 + j >= g.lo && e0 + j < g.valid) gout[g.gbase + e0 + j] = o.x[j];
-          }
+        } else {
+          if (excl_kind)
+            chain(std::true_type{});
+          else
+            chain(std::false_type{});
         }
+        store_segment(stage, g);
       } else if constexpr (LAY == 1) {
         // lane-blocked: this lane's row of CH chunks, one warp scan of the row
         // totals, results written back in place, then streamed out striped
@@ -946,23 +993,7 @@ __global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel
           TileScan<Pol, NC, CH, V>::finish_chunk(pol, pc, a[c], excl_kind, o.x);
           *reinterpret_cast<uint4*>(stage + size_t(r0 + c * V) * sizeof(in_t)) = o.u;
         }
-        __syncwarp();
-#pragma unroll
-        for (int c = 0; c < CH; ++c) {
-          const int e0 = w * Cfg::SEG + (c * 32 + lane) * V;
-          union {
-            uint4 u;
-            out_t x[V];
-          } o;
-          o.u = *reinterpret_cast<const uint4*>(stage + size_t(e0) * sizeof(in_t));
-          if (out_vec && e0 >= g.lo && e0 + V <= g.valid) {
-            ptx::st_stream_v4(gout + (g.gbase + e0), o.u);
-          } else {
-#pragma unroll
-            for (int j = 0; j < V; ++j)
-              if (e0 + j >= g.lo && e0 + j < g.valid) gout[g.gbase + e0 + j] = o.x[j];
-          }
-        }
+        store_segment(stage, g);
       } else {
       acc_t X = pol.aid();
       // chunks in groups of SG: the SG warp scans of a group are independent
@@ -1012,6 +1043,7 @@ __global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel
       have = have_next;
     }
   }
+  if constexpr (BS != 0) ptx::bulk_wait<0>();  // this thread's bulk stores are complete
   __syncthreads();
   if (threadIdx.x == 0) cta_exit_rearm(hdr, args.desc, uint64_t(ntiles) * codec::W);
 }

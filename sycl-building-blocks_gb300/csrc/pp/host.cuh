@@ -21,6 +21,7 @@
 #include "cooperative_scan.cuh"
 #include "decoupled_scan.cuh"
 #include "reduce.cuh"
+#include "rows.cuh"
 #include "scan_policy.cuh"
 #include "segmented.cuh"
 #include "workspace.cuh"
@@ -237,7 +238,9 @@ struct tune_kind<F64CarryF32> {
 //   int4         striped 64 KB tiles, ticket one stage life ahead;
 //   float4       rows of 9 chunks (72 KB tiles), late ticket, two polls;
 //   wide8        lane-blocked rows of 9 chunks (72 KB), late ticket, two polls;
-//   compensated  rows of 7 chunks over 20 warps (70 KB), late ticket, two polls;
+//   compensated  rows of 7 chunks over 20 warps (70 KB), late ticket, two polls,
+//                segments leave by bulk copy (the arithmetic, not the stores,
+//                bounds this one: stages are freed sooner);
 //   fp64_carry   as float4.
 template <class Pol>
 struct DecoupledTuning {
@@ -250,6 +253,7 @@ struct DecoupledTuning {
   static constexpr int LAY = kRows ? 2 : (K == TuneKind::wide8 ? 1 : 0);  // striped / blocked / rows
   static constexpr int TK = K == TuneKind::int4 ? 0 : 2;                  // when tickets are drawn
   static constexpr unsigned PG = K == TuneKind::int4 ? 0u : 250u;         // second poll delay (ns)
+  static constexpr int BS = K == TuneKind::compensated ? 1 : 0;          // bulk-copy stores of segments
   static constexpr int GEN_NC = 8;
   static constexpr int GEN_IPT = 8;
 };
@@ -330,7 +334,8 @@ inline Status decoupled_scan(cudaStream_t s, const void* in, void* out, uint64_t
   if constexpr (16 % sizeof(typename Pol::in_t) == 0) {
     if (tma_path_ok<Pol>(in, out)) {
       using Cfg = StagedFor<Pol>;
-      auto k = decoupled_staged_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Tn::LAY, Tn::TK, 0, Tn::PG>;
+      auto k = decoupled_staged_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Tn::LAY, Tn::TK, 0, Tn::PG, -1,
+                                       Tn::BS>;
       int bps = 0;
       st = prepare_kernel(k, Cfg::THREADS, Cfg::SMEM, bps);
       if (st != Status::ok) return st;
@@ -623,6 +628,31 @@ inline Status rows_scan(cudaStream_t s, const T* in, T* out, uint64_t rows, uint
   if (n == 0) return Status::ok;
   if (!in || !out) return Status::invalid_arg;
   if (!aligned16(in) || !aligned16(out)) return Status::invalid_arg;
+  DeviceInfo di;
+  Status st0 = device_info(di);
+  if (st0 != Status::ok) return st0;
+  // One warp per row when rows are long enough to stream and there are
+  // enough of them (or they are not too long); else rows are segments of the
+  // decoupled look-back kernel, which spreads long rows over many SMs.
+  if (cols >= 256 && (rows >= uint64_t(2 * di.sm_count) || cols <= (uint64_t(1) << 16))) {
+    constexpr int U = 8;
+    const bool vec = (cols * sizeof(T)) % 16 == 0;
+    auto launch = [&](auto kernel) -> Status {
+      int bps = 0;
+      Status st = prepare_kernel(kernel, 256, 0, bps);
+      if (st != Status::ok) return st;
+      uint64_t grid = (rows + 7) / 8;
+      const uint64_t cap = uint64_t(bps) * di.sm_count;
+      if (grid > cap) grid = cap;
+      kernel<<<unsigned(grid), 256, 0, s>>>(in, out, rows, cols, exclusive ? 1 : 0);
+      return from_cuda(cudaGetLastError());
+    };
+    constexpr int VV = 16 / int(sizeof(T));
+    if (reverse) {
+      return vec ? launch(rows_warp_kernel<T, Op, true, VV, U>) : launch(rows_warp_kernel<T, Op, true, 1, U>);
+    }
+    return vec ? launch(rows_warp_kernel<T, Op, false, VV, U>) : launch(rows_warp_kernel<T, Op, false, 1, U>);
+  }
   const SegWsLayout L = seg_ws_layout<T, Op>(n, 0, false, false);
   Ws w;
   Status st = acquire_ws(s, L.control_bytes, user_ws, user_ws_bytes, w);

@@ -7,7 +7,9 @@
 //   benchmarks/benchmark_scan.cpp - fill(1) -> out[n-1] == n
 //   tests/test_intrinsics.cpp - the intrinsics known answers, evaluated on
 //                               the GPU into a result buffer (no device traps)
-// plus a non-commutative user operator (affine-map composition).
+// plus a non-commutative user operator (affine-map composition) and the
+// subset grid barrier of cooperative_groups.hpp (membership by list and by
+// predicate, reuse across many phases, a wait that runs out of time).
 // Prints one line per check and exits non-zero on any failure.
 #include <cmath>
 #include <cstdio>
@@ -15,6 +17,7 @@
 #include <span>
 #include <vector>
 
+#include <parallel_primitives/cooperative_groups.hpp>
 #include <parallel_primitives/intrinsics.hpp>
 #include <parallel_primitives/reduction.hpp>
 #include <parallel_primitives/scan.hpp>
@@ -232,6 +235,136 @@ static void test_intrinsics() {
   cudaFree(d);
 }
 
+// ---- subset grid barrier (nd_range_barrier) ----------------------------------
+// Member blocks publish their phase number, cross the barrier, and check that
+// every other member has published at least that phase. Non-members leave.
+__global__ void barrier_phases_kernel(nd_range_barrier* b, unsigned* stamp, unsigned* errors, unsigned* ok_out,
+                                      int phases) {
+  const unsigned g = blockIdx.x;
+  const bool member = b->is_member();
+  for (int p = 1; p <= phases; ++p) {
+    if (member && threadIdx.x == 0) atomicExch(&stamp[g], unsigned(p));
+    if (!b->wait()) {
+      if (threadIdx.x == 0) ok_out[g] = 0u;
+      return;
+    }
+    if (member && threadIdx.x == 0) {
+      for (unsigned o = 0; o < gridDim.x; ++o) {
+        const unsigned v = atomicAdd(&stamp[o], 0u);
+        if (v != 0xFFFFFFFFu && v < unsigned(p)) atomicAdd(errors, 1u);
+      }
+    }
+  }
+  if (threadIdx.x == 0) ok_out[g] = 1u;
+}
+
+// Block 0 never arrives: the other members' waits run out of time.
+__global__ void barrier_missing_member_kernel(nd_range_barrier* b, unsigned* ok_out) {
+  if (blockIdx.x == 0) {
+    if (threadIdx.x == 0) ok_out[0] = 2u;
+    return;
+  }
+  const bool ok = b->wait();
+  if (threadIdx.x == 0) ok_out[blockIdx.x] = ok ? 1u : 0u;
+}
+
+static void run_phases(cudaStream_t s, nd_range_barrier* b, unsigned grid, const std::vector<bool>& member,
+                       const char* what) {
+  unsigned *stamp, *errors, *ok;
+  cudaMalloc(&stamp, grid * 4);
+  cudaMalloc(&errors, 4);
+  cudaMalloc(&ok, grid * 4);
+  std::vector<unsigned> init(grid);
+  for (unsigned g = 0; g < grid; ++g) init[g] = member[g] ? 0u : 0xFFFFFFFFu;  // non-members never publish
+  cudaMemcpy(stamp, init.data(), grid * 4, cudaMemcpyHostToDevice);
+  cudaMemset(errors, 0, 4);
+  cudaMemset(ok, 0, grid * 4);
+  int phases = 200;
+  void* args[] = {&b, &stamp, &errors, &ok, &phases};
+  const cudaError_t e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(barrier_phases_kernel), dim3(grid),
+                                                    dim3(128), args, 0, s);
+  CHECK(e == cudaSuccess, "%s: cooperative launch: %s", what, cudaGetErrorString(e));
+  cudaStreamSynchronize(s);
+  unsigned err = 0;
+  std::vector<unsigned> okh(grid);
+  cudaMemcpy(&err, errors, 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(okh.data(), ok, grid * 4, cudaMemcpyDeviceToHost);
+  unsigned done = 0;
+  for (unsigned g = 0; g < grid; ++g) done += okh[g];
+  CHECK(err == 0, "%s: %u members ran ahead of the barrier", what, err);
+  CHECK(done == grid, "%s: %u of %u blocks finished", what, done, grid);
+  CHECK(!nd_range_barrier::timed_out(b, s), "%s: barrier reports a timeout", what);
+  std::printf("barrier %s: %u blocks, 200 phases, ok\n", what, grid);
+  cudaFree(stamp);
+  cudaFree(errors);
+  cudaFree(ok);
+}
+
+static void test_barrier(cudaStream_t s) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const unsigned grid = unsigned(sms);
+  {  // every other block, by predicate
+    nd_range_barrier* b =
+        nd_range_barrier::make_barrier_if(s, dim3(grid), dim3(128), [](size_t g) { return g % 2 == 0; });
+    std::vector<bool> member(grid);
+    for (unsigned g = 0; g < grid; ++g) member[g] = g % 2 == 0;
+    run_phases(s, b, grid, member, "even blocks (predicate)");
+    nd_range_barrier::destroy(b);
+  }
+  {  // an explicit list, checked against the kernel's occupancy
+    std::vector<size_t> list = {1, 3, 4, 9, size_t(grid - 1)};
+    nd_range_barrier* b = nd_range_barrier::make_barrier_for(s, barrier_phases_kernel, dim3(grid), dim3(128), 0, list);
+    std::vector<bool> member(grid, false);
+    for (size_t g : list) member[g] = true;
+    run_phases(s, b, grid, member, "listed blocks");
+    nd_range_barrier::destroy(b);
+  }
+  {  // all blocks
+    nd_range_barrier* b = nd_range_barrier::make_barrier(s, dim3(grid), dim3(128));
+    run_phases(s, b, grid, std::vector<bool>(grid, true), "all blocks");
+    nd_range_barrier::destroy(b);
+  }
+  {  // a member that never arrives: the waits end with an error, the kernel ends
+    nd_range_barrier* b = nd_range_barrier::make_barrier(s, dim3(8), dim3(64), {}, 20000000ull);
+    unsigned* ok;
+    cudaMalloc(&ok, 8 * 4);
+    cudaMemset(ok, 0xFF, 8 * 4);
+    void* args[] = {&b, &ok};
+    const cudaError_t e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(barrier_missing_member_kernel),
+                                                      dim3(8), dim3(64), args, 0, s);
+    CHECK(e == cudaSuccess, "timeout launch: %s", cudaGetErrorString(e));
+    CHECK(cudaStreamSynchronize(s) == cudaSuccess, "timeout kernel did not finish cleanly");
+    std::vector<unsigned> okh(8);
+    cudaMemcpy(okh.data(), ok, 8 * 4, cudaMemcpyDeviceToHost);
+    CHECK(okh[0] == 2u, "block 0 did not leave");
+    for (int g = 1; g < 8; ++g) CHECK(okh[g] == 0u, "block %d: wait did not report the timeout (%u)", g, okh[g]);
+    CHECK(nd_range_barrier::timed_out(b, s), "barrier does not report the timeout");
+    std::printf("barrier timeout: waits returned false, error recorded\n");
+    cudaFree(ok);
+    nd_range_barrier::destroy(b);
+  }
+  {  // host-side checks (perform_check): out-of-range member, oversized grid
+    bool threw = false;
+    try {
+      nd_range_barrier::make_barrier(s, dim3(4), dim3(32), {7});
+    } catch (const error&) {
+      threw = true;
+    }
+    CHECK(threw, "out-of-range member accepted");
+    threw = false;
+    try {
+      nd_range_barrier::make_barrier(s, dim3(grid * 1000), dim3(32));
+    } catch (const error& e) {
+      threw = e.status == pp::host::Status::grid_too_large;
+    }
+    CHECK(threw, "oversized grid accepted");
+    const dim3 occ = get_max_occupancy(barrier_phases_kernel, 128);
+    CHECK(occ.x >= grid, "get_max_occupancy %u < SMs", occ.x);
+  }
+}
+
 int main() {
   cudaStream_t s;
   cudaStreamCreate(&s);
@@ -242,6 +375,7 @@ int main() {
     test_basel(s);
     test_wallis(s);
     test_user_functor(s);
+    test_barrier(s);
   } catch (const std::exception& e) {
     std::printf("FAIL exception: %s\n", e.what());
     ++failures;

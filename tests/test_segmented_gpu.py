@@ -89,7 +89,11 @@ def test_segmented_reduce(pp, oracle, cuda, dtype, op):
 
 
 @pytest.mark.parametrize("dtype", ["f32", "i32", "u64", "f64"])
-@pytest.mark.parametrize("shape", [(1, 1), (3, 5), (2, 16384), (7, 16385), (5, 20001), (64, 256), (33, 4096)])
+# rows of >= 256 elements go one warp per row (vector steps when rows are 16-byte
+# multiples, scalar otherwise); shorter rows, and few rows longer than 65536,
+# are segments of the decoupled look-back kernel
+@pytest.mark.parametrize("shape", [(1, 1), (3, 5), (40, 255), (2, 16384), (7, 16385), (5, 20001), (64, 256), (33, 4096),
+                                   (640, 300), (3, 70001)])
 @pytest.mark.parametrize("reverse", [False, True])
 def test_rows_scan(pp, oracle, cuda, dtype, shape, reverse):
     rows, cols = shape
