@@ -315,6 +315,39 @@ def run_secondary(torch, pp, stream, args, d_in32, d_out32) -> dict:
             raise RuntimeError("device error in secondary benchmark")
         return round(nbytes * steps / (ms * 1e-3) / 1e9, 2)
 
+    # C1: n = 2^24 uint32 U[0, 255] (64 MiB, fits in the L2): L2 flushed before every launch, each launch timed
+    n24 = 1 << 24
+    gen24 = torch.Generator(device="cuda")
+    gen24.manual_seed(SEED + 24)
+    x24 = torch.randint(0, 256, (n24,), dtype=torch.int32, device="cuda", generator=gen24)
+    y24 = torch.empty_like(x24)
+    r24 = torch.empty(1, dtype=torch.int64, device="cuda")
+    flush = torch.empty(1 << 28, dtype=torch.uint8, device="cuda")  # 256 MiB, twice the L2
+
+    def flushed_rate(fn, nbytes, reps=10):
+        for _ in range(3):
+            fn()
+        total = 0.0
+        for _ in range(reps):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            total += a.elapsed_time(b)
+        if pp.stream_status(sh) != 0:
+            raise RuntimeError("device error in the 2^24 benchmark")
+        return round(nbytes * reps / (total * 1e-3) / 1e9, 2)
+
+    out["u32_inclusive_plus_2p24_l2_flushed"] = flushed_rate(
+        lambda: pp.decoupled_scan_device("inclusive", "plus", x24.data_ptr(), y24.data_ptr(), n24, "u32", stream=sh),
+        8 * n24)
+    out["u32_sum_reduce_2p24_l2_flushed"] = flushed_rate(
+        lambda: pp.reduce("plus", x24.data_ptr(), n24, "u32", r24.data_ptr(), stream=sh), 4 * n24)
+    del x24, y24, flush
+
     out["u32_exclusive_plus_2p30"] = rate(
         lambda: pp.decoupled_scan_device("exclusive", "plus", d_in32.data_ptr(), d_out32.data_ptr(), n30, "u32",
                                          stream=sh), 8 * n30)

@@ -479,6 +479,15 @@ struct SegTuning {
 template <class T, class Op>
 using SegCfgFor = SegCfg<SegPlainScan<T, Op>, SegTuning<T>::NC, SegTuning<T>::CH, SegTuning<T>::STAGES,
                          SegTuning<T>::LBW, SegTuning<T>::VB>;
+// Forward scans and reductions over CSR heads: lane rows of 9 16-byte chunks
+// over 14 warps (63 KB tiles), row totals kept for a thread-serial scan pass.
+template <class T>
+struct SegRowsTuning {
+  static constexpr int NC = 14, CH = 9, STAGES = 3, LBW = 4, VB = 16, LAY = 2;
+};
+template <class T, class Op>
+using SegCfgCsr = SegCfg<SegPlainScan<T, Op>, SegRowsTuning<T>::NC, SegRowsTuning<T>::CH, SegRowsTuning<T>::STAGES,
+                         SegRowsTuning<T>::LBW, SegRowsTuning<T>::VB, SegRowsTuning<T>::LAY>;
 
 // Control workspace: header + descriptors (room for both the segmented pass
 // and the rank scan of a reduce). Scratch workspace (a separate buffer, so
@@ -491,8 +500,11 @@ struct SegWsLayout {
 template <class T, class Op>
 inline SegWsLayout seg_ws_layout(uint64_t n, uint64_t num_segments, bool csr, bool reduce) {
   using Cfg = SegCfgFor<T, Op>;
+  using CfgC = SegCfgCsr<T, Op>;
+  constexpr uint64_t kTile = uint64_t(Cfg::TILE < CfgC::TILE ? Cfg::TILE : CfgC::TILE);
+  constexpr uint64_t kMap = uint64_t(Cfg::MAP_BYTES > CfgC::MAP_BYTES ? Cfg::MAP_BYTES : CfgC::MAP_BYTES);
   SegWsLayout L{};
-  const uint64_t ntiles = (n + Cfg::TILE - 1) / Cfg::TILE;
+  const uint64_t ntiles = (n + kTile - 1) / kTile;
   uint64_t words = ntiles * desc_codec<typename SegPlainScan<T, Op>::carry_t>::W;
   if (reduce) {
     const uint64_t rt = (num_segments + StagedFor<PlainScan<uint32_t, plus>>::TILE - 1) /
@@ -502,7 +514,7 @@ inline SegWsLayout seg_ws_layout(uint64_t n, uint64_t num_segments, bool csr, bo
   L.control_bytes = workspace_bytes_for_desc_words(words);
   size_t off = 0;
   L.bitmap_off = off;
-  L.bitmap_bytes = csr ? align_up(((n + 127) / 128) * 16 + Cfg::MAP_BYTES, 256) : 0;
+  L.bitmap_bytes = csr ? align_up(((n + 127) / 128) * 16 + kMap, 256) : 0;
   off += L.bitmap_bytes;
   L.nonempty_off = off;
   if (reduce) off += align_up(num_segments * 4, 256);
@@ -523,9 +535,11 @@ inline Status acquire_scratch(cudaStream_t s, size_t need, unsigned char** out) 
 
 template <class Pol, class Heads, bool REVERSE, bool REDUCE>
 inline Status launch_segmented(cudaStream_t s, const SegArgs& a) {
-  using Tn = SegTuning<typename Pol::in_t>;
-  using Cfg = SegCfg<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Tn::VB>;
-  auto k = segmented_staged_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Heads, REVERSE, REDUCE, Tn::VB>;
+  constexpr bool kRows = Heads::kBitmap && !REVERSE;
+  using Tn = std::conditional_t<kRows, SegRowsTuning<typename Pol::in_t>, SegTuning<typename Pol::in_t>>;
+  constexpr int LAY = kRows ? 2 : 0;
+  using Cfg = SegCfg<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Tn::VB, LAY>;
+  auto k = segmented_staged_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Heads, REVERSE, REDUCE, Tn::VB, LAY>;
   DeviceInfo di;
   Status st = device_info(di);
   if (st != Status::ok) return st;

@@ -82,7 +82,11 @@ struct SegArgs {
 
 // NC compute warps, CH chunks per lane, VB bytes per chunk (the vector width
 // of shared-memory loads and global stores: 4, 8 or 16), STAGES-deep ring.
-template <class Pol, int NC_, int CH_, int STAGES_, int LBW_, int VB_ = 16>
+// LAY 0: striped chunks (a warp scan per chunk); LAY 2: lane rows of CH
+// consecutive 16-byte chunks (CH odd: conflict-free), the reduce pass leaves
+// each row's (value, count) total in shared memory and the scan pass is one
+// thread-serial chain per row (forward scans and reductions with CSR heads).
+template <class Pol, int NC_, int CH_, int STAGES_, int LBW_, int VB_ = 16, int LAY_ = 0>
 struct SegCfg {
   using in_t = typename Pol::in_t;
   using acc_t = typename Pol::acc_t;
@@ -106,7 +110,10 @@ struct SegCfg {
   static constexpr size_t META_TAGG = META_PREF + align_up(sizeof(carry_t), 16);
   static constexpr size_t META_TILE = META_TAGG + align_up(sizeof(carry_t), 8);
   static constexpr size_t META_CNT = META_TILE + 8;
-  static constexpr size_t META_BYTES = align_up(META_CNT + 4, 16);
+  static constexpr int LAY = LAY_;
+  static_assert(LAY_ == 0 || (LAY_ == 2 && VB_ == 16 && (CH_ % 2) == 1), "rows need odd counts of 16-byte chunks");
+  static constexpr size_t META_ROWS = align_up(META_CNT + 4, 16);  // acc_t[NC * 32] row totals (LAY 2)
+  static constexpr size_t META_BYTES = align_up(META_ROWS + (LAY_ == 2 ? NC_ * 32 * sizeof(acc_t) : 0), 16);
   static constexpr size_t OFF_MAP = size_t(STAGES) * TILE_BYTES;
   static constexpr size_t OFF_META = OFF_MAP + size_t(STAGES) * MAP_BYTES;
   static constexpr size_t OFF_BAR = align_up(OFF_META + STAGES * META_BYTES, 8);
@@ -114,9 +121,11 @@ struct SegCfg {
 };
 
 // REDUCE: write only segment totals (via rank_to_seg) instead of the scan.
-template <class Pol, int NC, int CH, int STAGES, int LBW, class Heads, bool REVERSE, bool REDUCE, int VB = 16>
+template <class Pol, int NC, int CH, int STAGES, int LBW, class Heads, bool REVERSE, bool REDUCE, int VB = 16,
+          int LAY = 0>
 __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(const SegArgs sargs) {
-  using Cfg = SegCfg<Pol, NC, CH, STAGES, LBW, VB>;
+  using Cfg = SegCfg<Pol, NC, CH, STAGES, LBW, VB, LAY>;
+  static_assert(LAY == 0 || (!REVERSE && Heads::kBitmap), "rows: forward scans over CSR heads");
   using vec_t = std::conditional_t<VB == 16, uint4, std::conditional_t<VB == 8, uint2, uint32_t>>;
   using in_t = typename Pol::in_t;
   using out_t = typename Pol::out_t;
@@ -142,6 +151,7 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
   auto s_tile = [&](int s) { return reinterpret_cast<long long*>(meta(s) + Cfg::META_TILE); };
   auto s_cnt = [&](int s) { return reinterpret_cast<unsigned*>(meta(s) + Cfg::META_CNT); };
   auto s_map = [&](int s) { return reinterpret_cast<const uint32_t*>(smem + Cfg::OFF_MAP + size_t(s) * Cfg::MAP_BYTES); };
+  auto s_rows = [&](int s) { return reinterpret_cast<acc_t*>(meta(s) + Cfg::META_ROWS); };
 
   const Pol pol{};
   const int warp = threadIdx.x >> 5;
@@ -172,13 +182,15 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
       const uint64_t pol_l2 = ptx::policy_evict_first();
       const unsigned char* in = static_cast<const unsigned char*>(args.in);
       uint32_t pending = 0, pend_par = 0;
-      long long t = (long long)atomicAdd(&hdr->ticket, 1ull);
+      // tickets are drawn once a stage is free, so ticket order follows the
+      // order in which tiles reach their reduce pass
       for (int k = 0;; ++k) {
         const int s = k % STAGES;
         if (k >= STAGES) {
-          if (!mbar_wait_bounded(&empty[s], ((k / STAGES) - 1) & 1, hdr, tmo, (unsigned long long)t)) break;
+          if (!mbar_wait_bounded(&empty[s], ((k / STAGES) - 1) & 1, hdr, tmo, 0ull)) break;
           pending &= ~(1u << s);
         }
+        const long long t = (long long)atomicAdd(&hdr->ticket, 1ull);
         *s_tile(s) = t;
         if (t < ntiles) {
           const uint64_t base = uint64_t(phys(t)) * TILE;
@@ -199,7 +211,6 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
           } else {
             ptx::mbar_arrive(&full[s]);
           }
-          t = (long long)atomicAdd(&hdr->ticket, 1ull);
         } else {
           ptx::mbar_arrive(&full[s]);
           break;
@@ -217,24 +228,15 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
       if (!mbar_wait_bounded(&full[s], par, hdr, tmo, 0ull)) break;
       const long long tile = *s_tile(s);
       if (tile >= ntiles) break;
-      uint32_t peek_st = kInvalid;
-      carry_t peek_v = pol.cid();
-      if (lane == 0 && tile > 0) peek_st = codec::read(args.desc + (tile - 1) * codec::W, etag, peek_v);
-      if (!mbar_wait_bounded(&aggb[s], par, hdr, tmo, 0ull)) break;
-      const carry_t agg = *s_tagg(s);
-      uint64_t* d = args.desc + tile * codec::W;
+      // exclusive prefix from the predecessors' descriptors while the compute
+      // warps still reduce this tile (two polls in flight, 250 ns apart)
       carry_t excl = pol.cid();
-      bool ok = true;
       unsigned long long stats = 0;
-      if (tile == 0) {
-      } else if (__shfl_sync(kFullMask, peek_st, 0) == kPrefix) {
-        excl = shfl_idx(peek_v, 0);
-        if (lane == 0) codec::publish(d, pol.cop(excl, agg), make_tag(etag, kPrefix));
-      } else {
-        ok = lookback_multi<Pol, LBW>(pol, args.desc, tile, etag, hdr, tmo, lane, excl, stats);
-        if (ok && lane == 0) codec::publish(d, pol.cop(excl, agg), make_tag(etag, kPrefix));
-      }
-      if (!ok) break;
+      if (tile > 0 && !lookback_pipelined<Pol, LBW, 250u>(pol, args.desc, tile, etag, hdr, tmo, lane, excl, stats))
+        break;
+      if (!mbar_wait_bounded(&aggb[s], par, hdr, tmo, 0ull)) break;
+      if (tile > 0 && lane == 0)
+        codec::publish(args.desc + tile * codec::W, pol.cop(excl, *s_tagg(s)), make_tag(etag, kPrefix));
       if (lane == 0) {
         *s_pref(s) = excl;
         ptx::mbar_arrive(&prefb[s]);
@@ -324,6 +326,29 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
       bulk = int((uint32_t(valid * sizeof(in_t)) & ~15u) / sizeof(in_t));
       mt = Heads::kBitmap ? 0 : base % seg_len;
     };
+    // rows (LAY 2): V raw elements at tile offset e0 with their head bits
+    auto load_row_chunk = [&](int s, int e0, uint64_t base, int valid, int bulk, in_t (&x)[V]) -> uint32_t {
+      const unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
+      if (e0 + V <= bulk) {
+        union {
+          vec_t u;
+          in_t v[V];
+        } buf;
+        buf.u = *reinterpret_cast<const vec_t*>(stage + size_t(e0) * sizeof(in_t));
+#pragma unroll
+        for (int j = 0; j < V; ++j) x[j] = buf.v[j];
+      } else {
+#pragma unroll
+        for (int j = 0; j < V; ++j) {
+          const int p = e0 + j;
+          x[j] = p < bulk ? reinterpret_cast<const in_t*>(stage)[p]
+                          : (p < valid ? gin[base + p] : identity<decltype(pol.op), in_t>());
+        }
+      }
+      uint32_t hb = (s_map(s)[e0 >> 5] >> (e0 & 31)) & ((1u << V) - 1u);
+      if (e0 + V > valid) hb &= (e0 >= valid) ? 0u : ((1u << (valid - e0)) - 1u);
+      return hb;
+    };
     auto reduce_pass = [&](int k) -> bool {
       const int s = k % STAGES;
       if (!mbar_wait_bounded(&full[s], (k / STAGES) & 1, hdr, tmo, 0ull)) return false;
@@ -333,13 +358,27 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
       tile_geom(s, tile, base, valid, bulk, mt);
       if (tile >= ntiles) return false;
       acc_t r = pol.aid();
-      for (int c = 0; c < CH; ++c) {
-        in_t x[V];
-        const uint32_t hb = load_chunk(s, c, base, valid, bulk, mt, x);
-        acc_t t = pol.load(x[0], hb & 1u);
+      if constexpr (LAY == 2) {
+        // this lane's row in order; its (value, count) total stays for the scan pass
+        const int r0 = w * Cfg::SEG + lane * (CH * V);
 #pragma unroll
-        for (int j = 1; j < V; ++j) t = pol.aop(t, pol.load(x[j], (hb >> j) & 1u));
-        r = pol.aop(r, warp_reduce(t, aop, lane));
+        for (int c = 0; c < CH; ++c) {
+          in_t x[V];
+          const uint32_t hb = load_row_chunk(s, r0 + c * V, base, valid, bulk, x);
+#pragma unroll
+          for (int j = 0; j < V; ++j) r = pol.aop(r, pol.load(x[j], (hb >> j) & 1u));
+        }
+        s_rows(s)[w * 32 + lane] = r;
+        r = warp_reduce(r, aop, lane);
+      } else {
+        for (int c = 0; c < CH; ++c) {
+          in_t x[V];
+          const uint32_t hb = load_chunk(s, c, base, valid, bulk, mt, x);
+          acc_t t = pol.load(x[0], hb & 1u);
+#pragma unroll
+          for (int j = 1; j < V; ++j) t = pol.aop(t, pol.load(x[j], (hb >> j) & 1u));
+          r = pol.aop(r, warp_reduce(t, aop, lane));
+        }
       }
       unsigned last = 0;
       if (lane == 0) {
@@ -376,6 +415,90 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
       acc_t sx = (lane < w) ? s_aggs(s)[lane] : pol.aid();
       sx = warp_reduce(sx, aop, lane);
       const acc_t pw = w == 0 ? *s_pref(s) : pol.aop(*s_pref(s), sx);
+      if constexpr (LAY == 2) {
+        // one warp scan of the row totals, then a thread-serial chain per row
+        unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
+        const int r0 = w * Cfg::SEG + lane * (CH * V);
+        const acc_t rt = s_rows(s)[w * 32 + lane];
+        const acc_t inc = warp_inclusive_scan(rt, aop, lane);
+        acc_t ex = shfl_up(inc, 1);
+        if (lane == 0) ex = pol.aid();
+        acc_t p = pol.aop(pw, ex);
+        // head bit of the element after this row (next lane's first, or the
+        // next tile's first from the global bitmap)
+        bool next_head_after_row = false;
+        if constexpr (REDUCE) {
+          const int e1 = r0 + CH * V;
+          if (e1 < valid) {
+            next_head_after_row = (s_map(s)[e1 >> 5] >> (e1 & 31)) & 1u;
+          } else if (base + uint64_t(e1) < n) {
+            next_head_after_row = (__ldg(sargs.heads + ((base + uint64_t(e1)) >> 5)) >> ((base + e1) & 31)) & 1u;
+          }
+        }
+        uint32_t hb_next = 0;
+        in_t xn[V];
+        if constexpr (REDUCE) hb_next = load_row_chunk(s, r0, base, valid, bulk, xn);
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+          in_t x[V];
+          uint32_t hb;
+          if constexpr (REDUCE) {
+#pragma unroll
+            for (int j = 0; j < V; ++j) x[j] = xn[j];
+            hb = hb_next;
+            if (c + 1 < CH) hb_next = load_row_chunk(s, r0 + (c + 1) * V, base, valid, bulk, xn);
+          } else {
+            hb = load_row_chunk(s, r0 + c * V, base, valid, bulk, x);
+          }
+          const int e0 = r0 + c * V;
+          union {
+            vec_t u;
+            out_t v[V];
+          } o;
+#pragma unroll
+          for (int j = 0; j < V; ++j) {
+            const bool head = (hb >> j) & 1u;
+            const acc_t before = p;
+            p = pol.aop(p, pol.load(x[j], head));
+            if constexpr (!REDUCE) {
+              o.v[j] = excl_kind ? (head ? pol.aid().v : before.v) : p.v;
+            } else {
+              const int e = e0 + j;
+              if (e < valid) {
+                bool end;
+                if (base + uint64_t(e) + 1 >= n) end = true;
+                else if (j + 1 < V) end = (hb >> (j + 1)) & 1u;
+                else if (c + 1 < CH) end = hb_next & 1u;
+                else end = next_head_after_row;
+                if (end && p.c > 0) {
+                  const uint32_t seg = __ldg(sargs.rank_to_seg + (p.c - 1));
+                  static_cast<out_t*>(sargs.seg_out)[seg] = p.v;
+                }
+              }
+            }
+          }
+          if constexpr (!REDUCE) *reinterpret_cast<vec_t*>(stage + size_t(e0) * sizeof(in_t)) = o.u;
+        }
+        if constexpr (!REDUCE) {
+          __syncwarp();
+#pragma unroll
+          for (int c = 0; c < CH; ++c) {
+            const int e0 = w * Cfg::SEG + (c * 32 + lane) * V;
+            union {
+              vec_t u;
+              out_t v[V];
+            } o;
+            o.u = *reinterpret_cast<const vec_t*>(stage + size_t(e0) * sizeof(in_t));
+            if (e0 + V <= valid) {
+              ptx::st_stream<VB>(gout + base + e0, &o.u);
+            } else {
+#pragma unroll
+              for (int j = 0; j < V; ++j)
+                if (e0 + j < valid) gout[base + e0 + j] = o.v[j];
+            }
+          }
+        }
+      } else {
       acc_t X = pol.aid();
       for (int c = 0; c < CH; ++c) {
         in_t x[V];
@@ -458,6 +581,7 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
             }
           }
         }
+      }
       }
       __syncwarp();
       if (lane == 0) ptx::mbar_arrive(&empty[s]);
