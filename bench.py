@@ -369,6 +369,18 @@ def run_secondary(torch, pp, stream, args, d_in32, d_out32) -> dict:
             lambda k=kind: pp.decoupled_scan_device(k, "plus", u64.data_ptr(), o64.data_ptr(), n28, "u64", stream=sh),
             16 * n28)
     del u64, o64
+    # float64: every element costs FP64 additions, whose rate on this part is far below its HBM bandwidth
+    f64 = torch.randn(n28, dtype=torch.float64, device="cuda", generator=gen)
+    o64 = torch.empty_like(f64)
+    out["f64_inclusive_plus_2p28"] = rate(
+        lambda: pp.decoupled_scan_device("inclusive", "plus", f64.data_ptr(), o64.data_ptr(), n28, "f64", stream=sh),
+        16 * n28)
+    out["f64_sum_reduce_2p28"] = rate(
+        lambda: pp.reduce("plus", f64.data_ptr(), n28, "f64", o64.data_ptr(), stream=sh), 8 * n28)
+    out["f64_maximum_scan_2p28"] = rate(
+        lambda: pp.decoupled_scan_device("inclusive", "maximum", f64.data_ptr(), o64.data_ptr(), n28, "f64",
+                                         stream=sh), 16 * n28)
+    del f64, o64
     f = torch.randn(n30, dtype=torch.float32, device="cuda", generator=gen)
     res = torch.empty(2, dtype=torch.float32, device="cuda")
     out["f32_sum_reduce_2p30"] = rate(

@@ -214,7 +214,7 @@ inline Status prepare_kernel(K kernel, int threads, size_t smem, int& blocks_per
 // ---------------------------------------------------------------------------
 // Decoupled look-back scan.
 // Policy classes of the tuning table.
-enum class TuneKind { int4, float4, wide8, compensated, fp64_carry };
+enum class TuneKind { int4, float4, wide8, float8, compensated, fp64_carry };
 template <class Pol>
 struct tune_kind {
   static constexpr TuneKind value = TuneKind::int4;
@@ -222,7 +222,9 @@ struct tune_kind {
 template <class T, class Op>
 struct tune_kind<PlainScan<T, Op>> {
   static constexpr TuneKind value =
-      sizeof(T) == 8 ? TuneKind::wide8 : (std::is_same_v<T, float> ? TuneKind::float4 : TuneKind::int4);
+      std::is_same_v<T, double>
+          ? TuneKind::float8
+          : (sizeof(T) == 8 ? TuneKind::wide8 : (std::is_same_v<T, float> ? TuneKind::float4 : TuneKind::int4));
 };
 template <>
 struct tune_kind<CompensatedF32> {
@@ -238,6 +240,9 @@ struct tune_kind<F64CarryF32> {
 //   int4         striped 64 KB tiles, ticket one stage life ahead;
 //   float4       rows of 9 chunks (72 KB tiles), late ticket, two polls;
 //   wide8        lane-blocked rows of 9 chunks (72 KB), late ticket, two polls;
+//   float8       rows of 9 chunks over 14 warps (63 KB), late ticket, two polls:
+//                FP64 additions, not HBM, bound double scans on this part, and
+//                the row chains need the fewest of them;
 //   compensated  rows of 7 chunks over 20 warps (70 KB), late ticket, two polls,
 //                segments leave by bulk copy (the arithmetic, not the stores,
 //                bounds this one: stages are freed sooner);
@@ -245,8 +250,9 @@ struct tune_kind<F64CarryF32> {
 template <class Pol>
 struct DecoupledTuning {
   static constexpr TuneKind K = tune_kind<Pol>::value;
-  static constexpr bool kRows = K == TuneKind::float4 || K == TuneKind::compensated || K == TuneKind::fp64_carry;
-  static constexpr int NC = K == TuneKind::compensated ? 20 : 16;  // compute warps
+  static constexpr bool kRows = K == TuneKind::float4 || K == TuneKind::float8 || K == TuneKind::compensated ||
+                                K == TuneKind::fp64_carry;
+  static constexpr int NC = K == TuneKind::compensated ? 20 : (K == TuneKind::float8 ? 14 : 16);  // compute warps
   static constexpr int CH = K == TuneKind::int4 ? 8 : (K == TuneKind::compensated ? 7 : 9);  // chunks per lane
   static constexpr int STAGES = 3;  // shared-memory ring depth
   static constexpr int LBW = (K == TuneKind::float4 || K == TuneKind::fp64_carry) ? 2 : 4;  // windows per poll
@@ -464,30 +470,29 @@ inline Status reduce(cudaStream_t s, const T* in, uint64_t n, T* d_result, void*
 // Variant of the segmented kernel: 4-byte elements take the autotuned one
 // (seg_tuned.inc, written by ppautotune.py), others 16 warps x 16-byte chunks.
 #include "seg_tuned.inc"
-template <class T>
-struct SegTuning {
-  static constexpr bool k4 = sizeof(T) == 4;
-  static constexpr int NC = k4 ? PP_SEG_TUNED_4B_NC : 16;
-  static constexpr int VB = k4 ? PP_SEG_TUNED_4B_VB : 16;
-  static constexpr int ITEMS = k4 ? PP_SEG_TUNED_4B_ITEMS : 16;
-  static constexpr int CH = ITEMS / (VB / int(sizeof(T)));
-  static constexpr int TILE_BYTES = NC * 32 * ITEMS * int(sizeof(T));
-  static constexpr int STAGES = (196608 / TILE_BYTES) < 2 ? 2 : ((196608 / TILE_BYTES) > 8 ? 8 : (196608 / TILE_BYTES));
-  static constexpr int LBW = 4;
+// Variant of the segmented kernel. CSR forward scans and reductions take the
+// autotuned variant of their payload size and segment-length class (mean
+// length n / S >= kSegLongMean: "long"); row scans that fall back to this
+// kernel (uniform heads, either direction) take 16 warps of 8 16-byte chunks.
+constexpr uint64_t kSegLongMean = 512;
+template <int LAY_, int NC_, int CH_, int VB_, class T>
+struct SegVariant {
+  static constexpr int LAY = LAY_, NC = NC_, CH = CH_, VB = VB_, LBW = 4;
+  static constexpr int TILE_BYTES = NC * 32 * CH * VB;
+  static constexpr int ST0 = 196608 / TILE_BYTES;
+  static constexpr int STAGES = LAY == 2 ? 3 : (ST0 < 2 ? 2 : (ST0 > 8 ? 8 : ST0));
 };
-
-template <class T, class Op>
-using SegCfgFor = SegCfg<SegPlainScan<T, Op>, SegTuning<T>::NC, SegTuning<T>::CH, SegTuning<T>::STAGES,
-                         SegTuning<T>::LBW, SegTuning<T>::VB>;
-// Forward scans and reductions over CSR heads: lane rows of 9 16-byte chunks
-// over 14 warps (63 KB tiles), row totals kept for a thread-serial scan pass.
+template <class T, bool LONG>
+using SegTunedCsr = std::conditional_t<
+    sizeof(T) == 4,
+    std::conditional_t<LONG, SegVariant<PP_SEG_4B_LONG_LAY, PP_SEG_4B_LONG_NC, PP_SEG_4B_LONG_CH, PP_SEG_4B_LONG_VB, T>,
+                       SegVariant<PP_SEG_4B_SHORT_LAY, PP_SEG_4B_SHORT_NC, PP_SEG_4B_SHORT_CH, PP_SEG_4B_SHORT_VB, T>>,
+    std::conditional_t<LONG, SegVariant<PP_SEG_8B_LONG_LAY, PP_SEG_8B_LONG_NC, PP_SEG_8B_LONG_CH, PP_SEG_8B_LONG_VB, T>,
+                       SegVariant<PP_SEG_8B_SHORT_LAY, PP_SEG_8B_SHORT_NC, PP_SEG_8B_SHORT_CH, PP_SEG_8B_SHORT_VB, T>>>;
 template <class T>
-struct SegRowsTuning {
-  static constexpr int NC = 14, CH = 9, STAGES = 3, LBW = 4, VB = 16, LAY = 2;
-};
-template <class T, class Op>
-using SegCfgCsr = SegCfg<SegPlainScan<T, Op>, SegRowsTuning<T>::NC, SegRowsTuning<T>::CH, SegRowsTuning<T>::STAGES,
-                         SegRowsTuning<T>::LBW, SegRowsTuning<T>::VB, SegRowsTuning<T>::LAY>;
+using SegUniform = SegVariant<0, 16, 8, 16, T>;
+template <class Tn, class T, class Op>
+using SegCfgOf = SegCfg<SegPlainScan<T, Op>, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Tn::VB, Tn::LAY>;
 
 // Control workspace: header + descriptors (room for both the segmented pass
 // and the rank scan of a reduce). Scratch workspace (a separate buffer, so
@@ -499,10 +504,14 @@ struct SegWsLayout {
 };
 template <class T, class Op>
 inline SegWsLayout seg_ws_layout(uint64_t n, uint64_t num_segments, bool csr, bool reduce) {
-  using Cfg = SegCfgFor<T, Op>;
-  using CfgC = SegCfgCsr<T, Op>;
-  constexpr uint64_t kTile = uint64_t(Cfg::TILE < CfgC::TILE ? Cfg::TILE : CfgC::TILE);
-  constexpr uint64_t kMap = uint64_t(Cfg::MAP_BYTES > CfgC::MAP_BYTES ? Cfg::MAP_BYTES : CfgC::MAP_BYTES);
+  // sized for every variant a call may take
+  using C0 = SegCfgOf<SegUniform<T>, T, Op>;
+  using C1 = SegCfgOf<SegTunedCsr<T, true>, T, Op>;
+  using C2 = SegCfgOf<SegTunedCsr<T, false>, T, Op>;
+  constexpr uint64_t t01 = uint64_t(C0::TILE < C1::TILE ? C0::TILE : C1::TILE);
+  constexpr uint64_t kTile = t01 < uint64_t(C2::TILE) ? t01 : uint64_t(C2::TILE);
+  constexpr uint64_t m01 = uint64_t(C0::MAP_BYTES > C1::MAP_BYTES ? C0::MAP_BYTES : C1::MAP_BYTES);
+  constexpr uint64_t kMap = m01 > uint64_t(C2::MAP_BYTES) ? m01 : uint64_t(C2::MAP_BYTES);
   SegWsLayout L{};
   const uint64_t ntiles = (n + kTile - 1) / kTile;
   uint64_t words = ntiles * desc_codec<typename SegPlainScan<T, Op>::carry_t>::W;
@@ -533,13 +542,10 @@ inline Status acquire_scratch(cudaStream_t s, size_t need, unsigned char** out) 
   return st;
 }
 
-template <class Pol, class Heads, bool REVERSE, bool REDUCE>
-inline Status launch_segmented(cudaStream_t s, const SegArgs& a) {
-  constexpr bool kRows = Heads::kBitmap && !REVERSE;
-  using Tn = std::conditional_t<kRows, SegRowsTuning<typename Pol::in_t>, SegTuning<typename Pol::in_t>>;
-  constexpr int LAY = kRows ? 2 : 0;
-  using Cfg = SegCfg<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Tn::VB, LAY>;
-  auto k = segmented_staged_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Heads, REVERSE, REDUCE, Tn::VB, LAY>;
+template <class Tn, class Pol, class Heads, bool REVERSE, bool REDUCE>
+inline Status launch_segmented_variant(cudaStream_t s, const SegArgs& a) {
+  using Cfg = SegCfg<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Tn::VB, Tn::LAY>;
+  auto k = segmented_staged_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Heads, REVERSE, REDUCE, Tn::VB, Tn::LAY>;
   DeviceInfo di;
   Status st = device_info(di);
   if (st != Status::ok) return st;
@@ -553,6 +559,18 @@ inline Status launch_segmented(cudaStream_t s, const SegArgs& a) {
   if (ntiles < grid) grid = ntiles;
   k<<<unsigned(grid), Cfg::THREADS, Cfg::SMEM, s>>>(a);
   return from_cuda(cudaGetLastError());
+}
+
+template <class Pol, class Heads, bool REVERSE, bool REDUCE>
+inline Status launch_segmented(cudaStream_t s, const SegArgs& a, uint64_t num_segments = 0) {
+  using T = typename Pol::in_t;
+  if constexpr (Heads::kBitmap && !REVERSE) {
+    const bool long_segments = num_segments == 0 || a.s.n / num_segments >= kSegLongMean;
+    if (long_segments) return launch_segmented_variant<SegTunedCsr<T, true>, Pol, Heads, REVERSE, REDUCE>(s, a);
+    return launch_segmented_variant<SegTunedCsr<T, false>, Pol, Heads, REVERSE, REDUCE>(s, a);
+  } else {
+    return launch_segmented_variant<SegUniform<T>, Pol, Heads, REVERSE, REDUCE>(s, a);
+  }
 }
 
 inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
@@ -588,7 +606,7 @@ inline Status segmented_scan(cudaStream_t s, const T* in, T* out, uint64_t n, co
   a.s.debug_skip_tile = -1;
   a.s.exclusive = exclusive ? 1 : 0;
   a.heads = heads;
-  return launch_segmented<SegPlainScan<T, Op>, CsrHeads, false, false>(s, a);
+  return launch_segmented<SegPlainScan<T, Op>, CsrHeads, false, false>(s, a, num_segments);
 }
 
 // CSR segmented reduce: out[s] = op-reduction of segment s (identity if empty).
@@ -630,7 +648,7 @@ inline Status segmented_reduce(cudaStream_t s, const T* in, uint64_t n, const in
   a.heads = heads;
   a.rank_to_seg = r2s;
   a.seg_out = out;
-  return launch_segmented<SegPlainScan<T, Op>, CsrHeads, false, true>(s, a);
+  return launch_segmented<SegPlainScan<T, Op>, CsrHeads, false, true>(s, a, num_segments);
 }
 
 // Row scans of a rows x cols row-major matrix (every row its own segment);

@@ -1,13 +1,16 @@
 """Autotuner of the batched segmented scan.
 
-Compiles tune/seg_autotune.cu (every variant of the segmented kernel over
-compute warps {4, 8, 16} = block size {128, 256, 512} threads, items per
-thread {4, 8, 16, 32} and chunk vector width {4, 8, 16} bytes), runs it on the
-GPU on the batched workload (65,536 log-uniform segments, int32 and float32
-payloads), records every measurement in tune/seg_autotune_results.json and
-writes the variant with the best worst-case throughput over the two payloads
-to csrc/pp/seg_tuned.inc, which the library's segmented launches use for
-4-byte elements.
+Compiles tune/seg_autotune.cu (variants of the segmented kernel: striped
+chunks over compute warps {8, 16} = block size {256, 512} threads, items per
+thread {8, 16, 32} and chunk vector width {8, 16} bytes; lane rows over
+{12, 14, 16} warps with {5, 7, 9} 16-byte chunks per lane), runs it on the GPU
+on two length distributions ("long": 65,536 log-uniform segments in [1, 2^16];
+"short": 2^21 segments of U[1, 128]) with int32, float32, int64 and float64
+payloads, records every measurement in tune/seg_autotune_results.json and
+writes, per payload size (4 / 8 bytes) and distribution, the variant with the
+best worst-case throughput over that size's two payloads to
+csrc/pp/seg_tuned.inc. The library's CSR segmented launches pick the long or
+short variant from the mean segment length.
 
     python sycl-building-blocks_gb300/ppautotune.py
 """
@@ -36,7 +39,7 @@ def compile_tuner() -> Path:
 
 
 def run(exe: Path) -> list[dict]:
-    r = subprocess.run([str(exe)], capture_output=True, text=True, check=True, timeout=1200)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, check=True, timeout=2400)
     rows = []
     for line in r.stdout.splitlines():
         line = line.strip()
@@ -45,32 +48,43 @@ def run(exe: Path) -> list[dict]:
     return rows
 
 
+SIZES = {"i32": 4, "f32": 4, "i64": 8, "f64": 8}
+
+
 def choose(rows: list[dict]) -> dict:
+    """Best worst-case variant per (payload size, distribution)."""
     ok = [r for r in rows if "ms" in r and r.get("err") == 0 and r.get("matches_default")]
-    by_key: dict[tuple, dict] = {}
-    for r in ok:
-        by_key.setdefault((r["nc"], r["items"], r["vb"]), {})[r["dtype"]] = r
-    best, best_score = None, -1.0
-    for key, d in by_key.items():
-        if len(d) < 2:
-            continue
-        score = min(v["elems_per_s"] for v in d.values())
-        if score > best_score:
-            best, best_score = key, score
-    if best is None:
-        raise RuntimeError("no valid variant")
-    return {"nc": best[0], "items": best[1], "vb": best[2], "worst_case_elems_per_s": best_score}
+    out = {}
+    for size in (4, 8):
+        for dist in ("long", "short"):
+            by_key: dict[tuple, dict] = {}
+            for r in ok:
+                if SIZES[r["dtype"]] == size and r["dist"] == dist:
+                    by_key.setdefault((r["lay"], r["nc"], r["ch"], r["vb"]), {})[r["dtype"]] = r
+            best, best_score = None, -1.0
+            for key, d in by_key.items():
+                if len(d) < 2:
+                    continue
+                score = min(v["elems_per_s"] for v in d.values())
+                if score > best_score:
+                    best, best_score = key, score
+            if best is None:
+                raise RuntimeError(f"no valid variant for {size}-byte payloads, {dist} segments")
+            out[f"{size}B_{dist}"] = {"lay": best[0], "nc": best[1], "ch": best[2], "vb": best[3],
+                                      "worst_case_elems_per_s": best_score}
+    return out
 
 
 def write_inc(choice: dict, device: str) -> Path:
     inc = PKG / "csrc" / "pp" / "seg_tuned.inc"
-    inc.write_text(
-        "// Generated by ppautotune.py: segmented-scan variant with the best worst-case\n"
-        f"// throughput over int32 and float32 payloads on {device}, batched workload of\n"
-        "// 65,536 log-uniform segments (see tune/seg_autotune_results.json).\n"
-        f"#define PP_SEG_TUNED_4B_NC {choice['nc']}\n"
-        f"#define PP_SEG_TUNED_4B_ITEMS {choice['items']}\n"
-        f"#define PP_SEG_TUNED_4B_VB {choice['vb']}\n")
+    lines = ["// Generated by ppautotune.py: segmented-scan variants with the best worst-case",
+             f"// throughput per payload size and segment-length class on {device}",
+             "// (see tune/seg_autotune_results.json)."]
+    for key, c in choice.items():
+        size, dist = key.split("_")
+        for f in ("lay", "nc", "ch", "vb"):
+            lines.append(f"#define PP_SEG_{size}_{dist.upper()}_{f.upper()} {c[f]}")
+    inc.write_text("\n".join(lines) + "\n")
     return inc
 
 
