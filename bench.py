@@ -315,21 +315,24 @@ def run_secondary(torch, pp, stream, args, d_in32, d_out32) -> dict:
             raise RuntimeError("device error in secondary benchmark")
         return round(nbytes * steps / (ms * 1e-3) / 1e9, 2)
 
-    # C1: n = 2^24 uint32 U[0, 255] (64 MiB, fits in the L2): L2 flushed before every launch, each launch timed
+    # C1: n = 2^24 uint32 U[0, 255] (64 MiB, fits in the L2): L2 flushed (by a read) before every launch, each
+    # launch timed on its own
     n24 = 1 << 24
     gen24 = torch.Generator(device="cuda")
     gen24.manual_seed(SEED + 24)
     x24 = torch.randint(0, 256, (n24,), dtype=torch.int32, device="cuda", generator=gen24)
     y24 = torch.empty_like(x24)
     r24 = torch.empty(1, dtype=torch.int64, device="cuda")
-    flush = torch.empty(1 << 28, dtype=torch.uint8, device="cuda")  # 256 MiB, twice the L2
+    # reading 256 MiB (twice the L2) leaves the L2 full of clean lines of another buffer: no write-back of the
+    # flush itself lands in the timed launch
+    flush = torch.zeros(1 << 26, dtype=torch.int32, device="cuda")
 
     def flushed_rate(fn, nbytes, reps=10):
         for _ in range(3):
             fn()
         total = 0.0
         for _ in range(reps):
-            flush.zero_()
+            flush.sum()
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
             a.record(stream)
