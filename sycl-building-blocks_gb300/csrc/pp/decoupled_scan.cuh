@@ -535,6 +535,9 @@ __device__ __forceinline__ bool lookback_pipelined(const Pol& pol, const uint64_
 // PG: 0 = one look-back poll in flight; > 0 = two, the second PG ns later.
 // BS: 1 = in the row layouts each compute warp writes its finished segment
 // back with one bulk copy (shared -> global) instead of striped stores.
+// LA: how many tiles the compute warps reduce ahead of the one they scan (the
+// look-back of a tile has LA reduce passes and LA - 1 scan passes to finish);
+// needs STAGES >= LA + 2 to keep a load in flight.
 // EXC: -1 = scan kind read from the arguments; 0 / 1 = inclusive / exclusive
 // compiled in (one code path: smaller kernels for the instruction cache).
 // TK: when the producer draws the ticket of the next tile for a stage.
@@ -545,7 +548,7 @@ __device__ __forceinline__ bool lookback_pipelined(const Pol& pol, const uint64_
 // reach their reduce pass more closely, so predecessors' aggregates arrive
 // closer together; earlier ones hide the latency of the ticket atomic.
 template <class Pol, int NC, int CH, int STAGES, int LBW, int LAY = 0, int TK = 0, int NR = 0,
-          unsigned PG = 0, int EXC = -1, int BS = 0, class Trace = NoTrace>
+          unsigned PG = 0, int EXC = -1, int BS = 0, int LA = 1, class Trace = NoTrace>
 __global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel(const ScanArgs args) {
   using Cfg = StagedCfg<Pol, NC, CH, STAGES, LBW, LAY, NR>;
   using in_t = typename Pol::in_t;
@@ -880,7 +883,17 @@ __global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel
       for (int k = 0; reduce_pass(k); ++k) {
       }
     }
-    bool have = NR > 0 ? !reducer : reduce_pass(0);
+    static_assert(LA >= 1 && (LA == 1 || STAGES >= LA + 2), "reduce-ahead needs LA + 2 stages");
+    // reduce passes run LA tiles ahead of scan passes: nred tiles reduced so far
+    int nred = 0;
+    bool more = true;
+    if constexpr (NR == 0) {
+      while (more && nred < LA) {
+        more = reduce_pass(nred);
+        if (more) ++nred;
+      }
+    }
+    bool have = NR > 0 ? !reducer : nred > 0;
     for (int k = 0; have; ++k) {
       bool have_next = true;
       const int s = k % STAGES;
@@ -889,7 +902,11 @@ __global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel
         if (!mbar_wait_bounded(&full[s], (k / STAGES) & 1, hdr, tmo, 0ull)) break;
         if (*s_tile(s) >= ntiles) break;
       } else {
-        have_next = reduce_pass(k + 1);
+        if (more) {
+          more = reduce_pass(nred);
+          if (more) ++nred;
+        }
+        have_next = k + 1 < nred;
       }
       // scan pass of use k
       if constexpr (Trace::kOn)
