@@ -182,7 +182,7 @@ const char* pp_version(void);
  * Its scratch is a fixed 1 MiB array in the library's device image instead
  * of a cudaMalloc'd or per-stream cached workspace, so it allocates nothing.
  * Limit: n up to 1,870,659,581 elements of a 4-byte integer type,
- * 2,104,492,029 floats, 526,123,007 elements of an 8-byte integer type or
+ * 2,104,492,029 floats, 511,508,479 elements of an 8-byte integer type or
  * 460,357,631 doubles; larger n
  * returns PP_ERR_WORKSPACE. All calls share the
  * array: calls that overlap on the GPU race, so order them on one stream.

@@ -15,7 +15,7 @@
 //   * the scratch holds kNoAllocScratchBytes = 1 MiB, enough for 114,176
 //     descriptor words: up to 1,870,659,581 elements of a 4-byte integer type
 //     (16,384-element tiles, one word each), 2,104,492,029 floats (18,432-
-//     element tiles), 526,123,007 elements of an 8-byte integer type (9,216-
+//     element tiles), 511,508,479 elements of an 8-byte integer type (8,960-
 //     element tiles, two words each) and 460,357,631 doubles (8,064-element
 //     tiles, two words each); three, three, one and one elements more when
 //     the input is 16-byte aligned. Larger n is rejected with PP_ERR_WORKSPACE

@@ -250,7 +250,7 @@ struct pol_commutative<F64CarryF32> : std::true_type {};
 // CH odd in layouts 1 and 2: rows of CH * 16 bytes then start in 8 different
 // 16-byte bank groups for any 8 consecutive lanes, so row reads are free of
 // bank conflicts; results go back into the row and leave striped.
-template <class Pol, int NC_, int CH_, int STAGES_, int LBW_, int LAY_ = 0, int NR_ = 0>
+template <class Pol, int NC_, int CH_, int STAGES_, int LBW_, int LAY_ = 0, int NR_ = 0, int SW_ = 0>
 struct StagedCfg {
   using in_t = typename Pol::in_t;
   using acc_t = typename Pol::acc_t;
@@ -267,7 +267,8 @@ struct StagedCfg {
   static constexpr int TILE = NC * SEG;
   static constexpr int TILE_BYTES = TILE * int(sizeof(in_t));
   static constexpr int NR = NR_;            // reducer warps (0: the compute warps reduce too)
-  static constexpr int THREADS = (NC + NR + 2) * 32;
+  static constexpr int SW = SW_;            // store warps (1: a warp writes finished tiles back by bulk copy)
+  static constexpr int THREADS = (NC + NR + 2 + SW) * 32;
   // per-stage metadata
   static constexpr size_t META_AGG = 0;                                   // acc_t[NC] segment aggregates
   static constexpr size_t META_PREF = align_up(NC * sizeof(acc_t), 16);   // carry_t tile exclusive prefix
@@ -277,8 +278,8 @@ struct StagedCfg {
   static constexpr size_t META_ROWS = align_up(META_CNT + 4, 16);                  // acc_t[NC*32] row totals
   static constexpr size_t META_BYTES = align_up(META_ROWS + (LAY_ == 2 ? NC_ * 32 * sizeof(acc_t) : 0), 16);
   static constexpr size_t OFF_META = size_t(STAGES) * TILE_BYTES;
-  static constexpr size_t OFF_BAR = align_up(OFF_META + STAGES * META_BYTES, 8);  // 5 barriers / stage
-  static constexpr size_t SMEM = OFF_BAR + 5 * STAGES * 8;
+  static constexpr size_t OFF_BAR = align_up(OFF_META + STAGES * META_BYTES, 8);  // 6 barriers / stage
+  static constexpr size_t SMEM = OFF_BAR + 6 * STAGES * 8;
 };
 
 // Geometry of tile t in the staged kernel. The tile grid is shifted by `head`
@@ -534,7 +535,9 @@ __device__ __forceinline__ bool lookback_pipelined(const Pol& pol, const uint64_
 // delays the publication of the next aggregates.
 // PG: 0 = one look-back poll in flight; > 0 = two, the second PG ns later.
 // BS: 1 = in the row layouts each compute warp writes its finished segment
-// back with one bulk copy (shared -> global) instead of striped stores.
+// back with one bulk copy (shared -> global) instead of striped stores;
+// 2 = one extra store warp writes each finished tile back with one bulk copy
+// and frees the stage, so the compute warps never wait for stores.
 // LA: how many tiles the compute warps reduce ahead of the one they scan (the
 // look-back of a tile has LA reduce passes and LA - 1 scan passes to finish);
 // needs STAGES >= LA + 2 to keep a load in flight.
@@ -549,8 +552,10 @@ __device__ __forceinline__ bool lookback_pipelined(const Pol& pol, const uint64_
 // closer together; earlier ones hide the latency of the ticket atomic.
 template <class Pol, int NC, int CH, int STAGES, int LBW, int LAY = 0, int TK = 0, int NR = 0,
           unsigned PG = 0, int EXC = -1, int BS = 0, int LA = 1, class Trace = NoTrace>
-__global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel(const ScanArgs args) {
-  using Cfg = StagedCfg<Pol, NC, CH, STAGES, LBW, LAY, NR>;
+__global__ void __launch_bounds__((NC + NR + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
+    decoupled_staged_kernel(const ScanArgs args) {
+  using Cfg = StagedCfg<Pol, NC, CH, STAGES, LBW, LAY, NR, (BS == 2 ? 1 : 0)>;
+  static_assert(BS != 2 || (LAY >= 1 && NR == 0), "the store warp serves the row layouts");
   using in_t = typename Pol::in_t;
   using out_t = typename Pol::out_t;
   using acc_t = typename Pol::acc_t;
@@ -567,7 +572,8 @@ __global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel
   uint64_t* empty = bars + STAGES;
   uint64_t* aggb = bars + 2 * STAGES;
   uint64_t* prefb = bars + 3 * STAGES;
-  uint64_t* sgo = bars + 4 * STAGES;  // compute warp 0 starts the scan pass (TK == 1)
+  uint64_t* sgo = bars + 4 * STAGES;      // compute warp 0 starts the scan pass (TK == 1)
+  uint64_t* scanned = bars + 5 * STAGES;  // the compute warps' results are in the stage (BS == 2)
   auto meta = [&](int s) { return smem + Cfg::OFF_META + size_t(s) * Cfg::META_BYTES; };
   auto s_aggs = [&](int s) { return reinterpret_cast<acc_t*>(meta(s) + Cfg::META_AGG); };
   auto s_pref = [&](int s) { return reinterpret_cast<carry_t*>(meta(s) + Cfg::META_PREF); };
@@ -593,7 +599,8 @@ __global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       ptx::mbar_init(&full[s], 1);
-      ptx::mbar_init(&empty[s], NC);
+      ptx::mbar_init(&empty[s], BS == 2 ? 1 : NC);
+      ptx::mbar_init(&scanned[s], NC);
       ptx::mbar_init(&aggb[s], NR > 0 ? NR : NC);
       ptx::mbar_init(&prefb[s], 1);
       ptx::mbar_init(&sgo[s], 1);
@@ -695,6 +702,32 @@ __global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel
       }
       __syncwarp();
     }
+  } else if (BS == 2 && warp == NC + NR + 2) {
+    // ------------------------------------------------------------ store
+    // Each finished full tile leaves as one bulk copy; the stage is freed as
+    // soon as the copy has read it. Partial tiles and outputs that are not
+    // 16-byte aligned are stored by the compute warps themselves.
+    out_t* gout = static_cast<out_t*>(args.out);
+    const bool out_vec = ((reinterpret_cast<uintptr_t>(gout) - uintptr_t(head) * sizeof(out_t)) & 15u) == 0;
+    const uint64_t pol_l2 = ptx::policy_evict_first();
+    for (int k = 0;; ++k) {
+      const int s = k % STAGES;
+      const uint32_t par = (k / STAGES) & 1;
+      if (!mbar_wait_bounded(&full[s], par, hdr, tmo, 0ull)) break;
+      const long long tile = *s_tile(s);
+      if (tile >= ntiles) break;
+      if (!mbar_wait_bounded(&scanned[s], par, hdr, tmo, 0ull)) break;
+      const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(tile, n, head);
+      if (lane == 0) {
+        if (out_vec && g.lo == 0 && g.valid == TILE) {
+          ptx::bulk_s2g_hint(gout + g.gbase, smem + size_t(s) * Cfg::TILE_BYTES, uint32_t(Cfg::TILE_BYTES), pol_l2);
+          ptx::bulk_commit();
+          ptx::bulk_wait_read<0>();
+        }
+        ptx::mbar_arrive(&empty[s]);
+      }
+      __syncwarp();
+    }
   } else {
     // ------------------------------------------------------------ compute
     // split mode: warps 2..NR+1 reduce, the NC warps after them scan
@@ -758,7 +791,12 @@ __global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel
     // else striped 16-byte stores. Returns once the stage may be reused.
     auto store_segment = [&](const unsigned char* stage, const StagedGeom& g) {
       const int s0 = w * Cfg::SEG;
-      if (BS && out_vec && s0 >= g.lo && s0 + Cfg::SEG <= g.valid) {
+      if (BS == 2 && out_vec && g.lo == 0 && g.valid == TILE) {
+        // the store warp writes the whole tile once every segment is in
+        ptx::fence_proxy_async_smem();
+        return;
+      }
+      if (BS == 1 && out_vec && s0 >= g.lo && s0 + Cfg::SEG <= g.valid) {
         ptx::fence_proxy_async_smem();
         __syncwarp();
         if (lane == 0) {
@@ -1055,7 +1093,7 @@ __global__ void __launch_bounds__((NC + NR + 2) * 32, 1) decoupled_staged_kernel
       __syncwarp();
       if (lane == 0) {
         if (w == 0) trace_now(kTrSDone, tile);
-        ptx::mbar_arrive(&empty[s]);
+        ptx::mbar_arrive(BS == 2 ? &scanned[s] : &empty[s]);
       }
       have = have_next;
     }

@@ -237,35 +237,43 @@ struct tune_kind<F64CarryF32> {
 
 // Staged-kernel configuration per policy class, from sweeps of 2^32-byte
 // inputs on GB300 (all: 3 stages, one CTA per SM):
-//   int4         striped 64 KB tiles, ticket one stage life ahead;
-//   float4       rows of 9 chunks (72 KB tiles), late ticket, two polls;
-//   wide8        lane-blocked rows of 9 chunks (72 KB), late ticket, two polls;
-//   float8       rows of 9 chunks over 14 warps (63 KB), late ticket, two polls:
-//                FP64 additions, not HBM, bound double scans on this part, and
-//                the row chains need the fewest of them;
-//   compensated  rows of 7 chunks over 20 warps (70 KB), late ticket, two polls,
-//                segments leave by bulk copy (the arithmetic, not the stores,
-//                bounds this one: stages are freed sooner);
-//   fp64_carry   as float4.
+//   int4         striped 64 KB tiles, ticket one stage life ahead, one poll of
+//                4 windows of 32 descriptors;
+//   float4       rows of 9 chunks (72 KB), late ticket, two polls of one window;
+//   wide8        rows of 7 chunks over 20 warps (70 KB), late ticket, two polls
+//                of one window, a store warp;
+//   float8       rows of 9 chunks over 14 warps (63 KB), late ticket, two polls,
+//                a store warp: FP64 additions, not HBM, bound double scans on
+//                this part, and the row chains need the fewest of them;
+//   compensated  as wide8 (the arithmetic, not the stores, bounds this one:
+//                with the store warp the compute warps never wait for stores);
+//   fp64_carry   as float4, with a store warp.
 template <class Pol>
 struct DecoupledTuning {
   static constexpr TuneKind K = tune_kind<Pol>::value;
   static constexpr bool kRows = K == TuneKind::float4 || K == TuneKind::float8 || K == TuneKind::compensated ||
                                 K == TuneKind::fp64_carry;
-  static constexpr int NC = K == TuneKind::compensated ? 20 : (K == TuneKind::float8 ? 14 : 16);  // compute warps
-  static constexpr int CH = K == TuneKind::int4 ? 8 : (K == TuneKind::compensated ? 7 : 9);  // chunks per lane
+  static constexpr bool k20 = K == TuneKind::compensated || K == TuneKind::wide8;
+  static constexpr int NC = k20 ? 20 : (K == TuneKind::float8 ? 14 : 16);  // compute warps
+  static constexpr int CH = K == TuneKind::int4 ? 8 : (k20 ? 7 : 9);        // chunks per lane
   static constexpr int STAGES = 3;  // shared-memory ring depth
-  static constexpr int LBW = (K == TuneKind::float4 || K == TuneKind::fp64_carry) ? 2 : 4;  // windows per poll
-  static constexpr int LAY = kRows ? 2 : (K == TuneKind::wide8 ? 1 : 0);  // striped / blocked / rows
+  static constexpr int LBW = K == TuneKind::int4 ? 4 : 1;  // windows of 32 descriptors per poll
+  static constexpr int LAY = (kRows || K == TuneKind::wide8) ? 2 : 0;                  // striped / rows
   static constexpr int TK = K == TuneKind::int4 ? 0 : 2;                  // when tickets are drawn
   static constexpr unsigned PG = K == TuneKind::int4 ? 0u : 250u;         // second poll delay (ns)
-  static constexpr int BS = K == TuneKind::compensated ? 1 : 0;          // bulk-copy stores of segments
+  // stores: a store warp writes finished tiles back by bulk copy (compensated,
+  // FP64 carry, 8-byte integers), else the compute warps store striped
+  static constexpr int BS = (K == TuneKind::compensated || K == TuneKind::fp64_carry || K == TuneKind::wide8 ||
+                             K == TuneKind::float8)
+                                ? 2
+                                : 0;
   static constexpr int GEN_NC = 8;
   static constexpr int GEN_IPT = 8;
 };
 template <class Pol>
 using StagedFor = StagedCfg<Pol, DecoupledTuning<Pol>::NC, DecoupledTuning<Pol>::CH, DecoupledTuning<Pol>::STAGES,
-                            DecoupledTuning<Pol>::LBW, DecoupledTuning<Pol>::LAY>;
+                            DecoupledTuning<Pol>::LBW, DecoupledTuning<Pol>::LAY, 0,
+                            (DecoupledTuning<Pol>::BS == 2 ? 1 : 0)>;
 
 // The staged (bulk-copy) kernel takes any naturally aligned pointers of an
 // element type whose size divides 16 bytes; the tile grid is shifted so that

@@ -66,8 +66,8 @@ def test_workspace_size_is_host_only(pp):
     n = 1 << 30
     size = pp.workspace_size("decoupled", "u32", a, a, n)
     assert size == 4096 + 8192 * 16 + (n // 16384) * 8
-    # uint64: 72 KB tiles (9216 elements), two words each
-    assert pp.workspace_size("decoupled", "u64", a, a, n) == 4096 + 8192 * 16 + -(-n // 9216) * 16
+    # uint64: 70 KB tiles (8960 elements), two words each
+    assert pp.workspace_size("decoupled", "u64", a, a, n) == 4096 + 8192 * 16 + -(-n // 8960) * 16
     # float: 72 KB tiles (18432 elements), one word each
     assert pp.workspace_size("decoupled", "f32", a, a, n) == 4096 + 8192 * 16 + -(-n // 18432) * 8
     # 4-byte but not 16-byte aligned input: the staged kernel's grid shifts by the phantom elements
