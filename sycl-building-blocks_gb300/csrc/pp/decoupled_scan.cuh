@@ -270,12 +270,12 @@ struct StagedCfg {
   static constexpr int SW = SW_;            // store warps (1: a warp writes finished tiles back by bulk copy)
   static constexpr int THREADS = (NC + NR + 2 + SW) * 32;
   // per-stage metadata
-  static constexpr size_t META_AGG = 0;                                   // acc_t[NC] segment aggregates
+  static constexpr size_t META_AGG = 0;  // acc_t[NC] segment aggregates, then their exclusive prefixes
   static constexpr size_t META_PREF = align_up(NC * sizeof(acc_t), 16);   // carry_t tile exclusive prefix
   static constexpr size_t META_TAGG = META_PREF + align_up(sizeof(carry_t), 16);  // carry_t tile aggregate
   static constexpr size_t META_TILE = META_TAGG + align_up(sizeof(carry_t), 8);   // long long tile index
   static constexpr size_t META_CNT = META_TILE + 8;                                // unsigned arrivals
-  static constexpr size_t META_ROWS = align_up(META_CNT + 4, 16);                  // acc_t[NC*32] row totals
+  static constexpr size_t META_ROWS = align_up(META_CNT + 4, 16);  // acc_t[NC*32] row prefixes in the segment
   static constexpr size_t META_BYTES = align_up(META_ROWS + (LAY_ == 2 ? NC_ * 32 * sizeof(acc_t) : 0), 16);
   static constexpr size_t OFF_META = size_t(STAGES) * TILE_BYTES;
   static constexpr size_t OFF_BAR = align_up(OFF_META + STAGES * META_BYTES, 8);  // 6 barriers / stage
@@ -829,7 +829,9 @@ __global__ void __launch_bounds__((NC + NR + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
     auto reduce_segment = [&](int s, int seg, const StagedGeom& g) -> acc_t {
       acc_t r = pol.aid();
       if constexpr (LAY == 2) {
-        // this lane's row, in order; the row total stays for the scan pass
+        // this lane's row, in order; the scan of the row totals over the
+        // segment is done here, off the scan pass's critical path, and the
+        // row's exclusive prefix stays for the scan pass
         const int r0 = seg * Cfg::SEG + lane * (CH * V);
         const bool interior = g.lo == 0 && g.blo == 0 && g.bhi == TILE;
 #pragma unroll
@@ -839,8 +841,10 @@ __global__ void __launch_bounds__((NC + NR + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
 #pragma unroll
           for (int j = 0; j < V; ++j) r = pol.aop_in(r, x[j]);
         }
-        s_rows(s)[seg * 32 + lane] = r;
-        r = warp_reduce(r, aop, lane);
+        const acc_t inc = warp_inclusive_scan(r, aop, lane);
+        const acc_t ex = shfl_up(inc, 1);
+        s_rows(s)[seg * 32 + lane] = lane == 0 ? pol.aid() : ex;
+        r = shfl_idx(inc, 31);
       } else if constexpr (pol_commutative<Pol>::value) {
         // V independent accumulators: short dependency chains
         acc_t rv[V];
@@ -871,7 +875,8 @@ __global__ void __launch_bounds__((NC + NR + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
     // Records the aggregate of segment seg. The warp that records the last
     // segment of the tile combines them and publishes the tile aggregate at
     // once (tile 0: its inclusive prefix), so successors never wait for this
-    // CTA's look-back of an earlier tile.
+    // CTA's look-back of an earlier tile; it leaves each segment's exclusive
+    // prefix inside the tile in place of its aggregate for the scan pass.
     auto record_segment = [&](int s, int seg, long long tile, const acc_t& r) {
       unsigned last = 0;
       if (lane == 0) {
@@ -883,6 +888,8 @@ __global__ void __launch_bounds__((NC + NR + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
         __threadfence_block();
         acc_t x = lane < NC ? s_aggs(s)[lane] : pol.aid();
         x = warp_inclusive_scan(x, aop, lane);
+        const acc_t xe = shfl_up(x, 1);
+        if (lane < NC) s_aggs(s)[lane] = lane == 0 ? pol.aid() : xe;
         const carry_t agg = pol.to_carry(shfl_idx(x, NC - 1));
         if (lane == 0) {
           *s_tagg(s) = agg;
@@ -955,32 +962,31 @@ __global__ void __launch_bounds__((NC + NR + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
       const long long tile = *s_tile(s);
       if (w == 0 && lane == 0) trace_now(kTrSStart, tile);
       const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(tile, n, head);
-      // exclusive prefix of this warp's segment inside the tile
-      acc_t sx = (lane < w) ? s_aggs(s)[lane] : pol.aid();
-      sx = warp_reduce(sx, aop, lane);
+      // exclusive prefix of this warp's segment inside the tile (left by the
+      // reduce pass)
+      const acc_t sx = s_aggs(s)[w];
       const pre_t pw = pol.prepare(w == 0 ? *s_pref(s) : pol.cop(*s_pref(s), pol.to_carry(sx)));
       if constexpr (LAY == 2) {
-        // rows: the row totals come from the reduce pass; one warp scan of
-        // them, then a thread-serial chain along the row
+        // rows: each row's prefix inside the segment comes from the reduce
+        // pass; a thread-serial chain along the row
         unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
         const int r0 = w * Cfg::SEG + lane * (CH * V);
         const bool interior = g.lo == 0 && g.blo == 0 && g.bhi == TILE;
-        const acc_t rt = s_rows(s)[w * 32 + lane];
-        const acc_t inc = warp_inclusive_scan(rt, aop, lane);
-        acc_t ex = shfl_up(inc, 1);
-        if (lane == 0) ex = pol.aid();
+        const acc_t ex = s_rows(s)[w * 32 + lane];
         typename Pol::row_t row = pol.row_start(pol.extend(pw, ex));
         auto chain = [&](auto excl_c) {
+          constexpr bool kEx = decltype(excl_c)::value;
+          union Out {
+            uint4 u;
+            out_t x[V];
+          };
 #pragma unroll
           for (int c = 0; c < CH; ++c) {
             in_t x[V];
             load_raw_at(s, r0 + c * V, g, interior, x);
-            union {
-              uint4 u;
-              out_t x[V];
-            } o;
+            Out o;
 #pragma unroll
-            for (int j = 0; j < V; ++j) o.x[j] = decltype(excl_c)::value ? pol.row_excl(row, x[j]) : pol.row_incl(row, x[j]);
+            for (int j = 0; j < V; ++j) o.x[j] = kEx ? pol.row_excl(row, x[j]) : pol.row_incl(row, x[j]);
             *reinterpret_cast<uint4*>(stage + size_t(r0 + c * V) * sizeof(in_t)) = o.u;
           }
         };

@@ -112,7 +112,7 @@ struct SegCfg {
   static constexpr size_t META_CNT = META_TILE + 8;
   static constexpr int LAY = LAY_;
   static_assert(LAY_ == 0 || (LAY_ == 2 && VB_ == 16 && (CH_ % 2) == 1), "rows need odd counts of 16-byte chunks");
-  static constexpr size_t META_ROWS = align_up(META_CNT + 4, 16);  // acc_t[NC * 32] row totals (LAY 2)
+  static constexpr size_t META_ROWS = align_up(META_CNT + 4, 16);  // acc_t[NC * 32] row prefixes (LAY 2)
   static constexpr size_t META_BYTES = align_up(META_ROWS + (LAY_ == 2 ? NC_ * 32 * sizeof(acc_t) : 0), 16);
   static constexpr size_t OFF_MAP = size_t(STAGES) * TILE_BYTES;
   static constexpr size_t OFF_META = OFF_MAP + size_t(STAGES) * MAP_BYTES;
@@ -359,7 +359,9 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
       if (tile >= ntiles) return false;
       acc_t r = pol.aid();
       if constexpr (LAY == 2) {
-        // this lane's row in order; its (value, count) total stays for the scan pass
+        // this lane's row in order; the scan of the (value, count) row totals
+        // over the segment is done here, and each row's exclusive prefix stays
+        // for the scan pass
         const int r0 = w * Cfg::SEG + lane * (CH * V);
 #pragma unroll
         for (int c = 0; c < CH; ++c) {
@@ -368,8 +370,10 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
 #pragma unroll
           for (int j = 0; j < V; ++j) r = pol.aop(r, pol.load(x[j], (hb >> j) & 1u));
         }
-        s_rows(s)[w * 32 + lane] = r;
-        r = warp_reduce(r, aop, lane);
+        const acc_t inc = warp_inclusive_scan(r, aop, lane);
+        const acc_t ex = shfl_up(inc, 1);
+        s_rows(s)[w * 32 + lane] = lane == 0 ? pol.aid() : ex;
+        r = shfl_idx(inc, 31);
       } else {
         for (int c = 0; c < CH; ++c) {
           in_t x[V];
@@ -390,6 +394,9 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
         __threadfence_block();
         acc_t x = lane < NC ? s_aggs(s)[lane] : pol.aid();
         x = warp_inclusive_scan(x, aop, lane);
+        // each segment's exclusive prefix inside the tile replaces its aggregate
+        const acc_t xe = shfl_up(x, 1);
+        if (lane < NC) s_aggs(s)[lane] = lane == 0 ? pol.aid() : xe;
         const carry_t agg = pol.to_carry(shfl_idx(x, NC - 1));
         if (lane == 0) {
           *s_tagg(s) = agg;
@@ -412,18 +419,13 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
       uint64_t base, mt;
       int valid, bulk;
       tile_geom(s, tile, base, valid, bulk, mt);
-      acc_t sx = (lane < w) ? s_aggs(s)[lane] : pol.aid();
-      sx = warp_reduce(sx, aop, lane);
-      const acc_t pw = w == 0 ? *s_pref(s) : pol.aop(*s_pref(s), sx);
+      const acc_t pw = w == 0 ? *s_pref(s) : pol.aop(*s_pref(s), s_aggs(s)[w]);
       if constexpr (LAY == 2) {
-        // one warp scan of the row totals, then a thread-serial chain per row
+        // the row's prefix inside the segment comes from the reduce pass; a
+        // thread-serial chain per row
         unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
         const int r0 = w * Cfg::SEG + lane * (CH * V);
-        const acc_t rt = s_rows(s)[w * 32 + lane];
-        const acc_t inc = warp_inclusive_scan(rt, aop, lane);
-        acc_t ex = shfl_up(inc, 1);
-        if (lane == 0) ex = pol.aid();
-        acc_t p = pol.aop(pw, ex);
+        acc_t p = pol.aop(pw, s_rows(s)[w * 32 + lane]);
         // head bit of the element after this row (next lane's first, or the
         // next tile's first from the global bitmap)
         bool next_head_after_row = false;
