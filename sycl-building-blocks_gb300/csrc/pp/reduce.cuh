@@ -8,7 +8,8 @@
 // loads (UNROLL independent loads in flight per thread, V accumulators per
 // thread to break dependency chains), reduces warps with shuffles and blocks
 // through shared memory, and the last block to finish folds the per-block
-// partials in block order and writes the result to device memory. For a
+// partials (all its threads, then a block reduction) and writes the result to
+// device memory. For a
 // fixed grid the combine order is fixed, so floating-point results are
 // reproducible run to run. As with sycl::reduction, the operator must be
 // associative and commutative.
@@ -132,20 +133,16 @@ __global__ void __launch_bounds__(BLOCK) reduce_kernel(const ReduceArgs args) {
   }
   __syncthreads();
   if (!s_last) return;
-  // last block: fold the partials in block order
+  // last block: every thread folds its share of the partials (one round trip
+  // to the L2 instead of one per 32 blocks), then one block reduction; the
+  // order is fixed for a fixed grid
   __threadfence();
   T r = identity<Op, T>();
-  const int lane = threadIdx.x & 31;
-  if (threadIdx.x < 32) {
-    for (unsigned b0 = 0; b0 < gridDim.x; b0 += 32) {
-      const unsigned b = b0 + lane;
-      T x = b < gridDim.x ? ld_cg(partials + size_t(b) * STRIDE) : identity<Op, T>();
-      r = op(r, warp_reduce(x, op, lane));
-    }
-    if (lane == 0) {
-      *static_cast<T*>(args.result) = r;
-      args.hdr->done = 0u;
-    }
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += BLOCK) r = op(r, ld_cg(partials + size_t(b) * STRIDE));
+  r = block_reduce<T, Op, BLOCK>(r, op, s_warp);
+  if (threadIdx.x == 0) {
+    *static_cast<T*>(args.result) = r;
+    args.hdr->done = 0u;
   }
 }
 

@@ -1,9 +1,10 @@
 """Autotuner of the batched segmented scan.
 
-Compiles tune/seg_autotune.cu (variants of the segmented kernel: striped
-chunks over compute warps {8, 16} = block size {256, 512} threads, items per
-thread {8, 16, 32} and chunk vector width {8, 16} bytes; lane rows over
-{12, 14, 16} warps with {5, 7, 9} 16-byte chunks per lane), runs it on the GPU
+Compiles tune/seg_autotune.cu once per payload type, in parallel (variants of
+the segmented kernel: striped chunks over compute warps {4, 8, 16} = block size
+{128, 256, 512} threads, items per thread {4, 8, 16, 32} and chunk vector width
+{8, 16} bytes; lane rows over {12, 14, 16, 18, 20} warps with {5, 7, 9} 16-byte
+chunks per lane), runs the binaries one after another on the GPU
 on two length distributions ("long": 65,536 log-uniform segments in [1, 2^16];
 "short": 2^21 segments of U[1, 128]) with int32, float32, int64 and float64
 payloads, records every measurement in tune/seg_autotune_results.json and
@@ -28,23 +29,32 @@ PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 
 
-def compile_tuner() -> Path:
-    out = PKG / "_build" / "seg_autotune"
-    out.parent.mkdir(exist_ok=True)
+def compile_tuners() -> list[Path]:
+    """One binary per payload type (int32, float32, int64, float64), compiled in parallel."""
+    (PKG / "_build").mkdir(exist_ok=True)
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    cmd = [nvcc, "-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "--expt-extended-lambda",
-           "-I", str(PKG / "csrc"), "-I", str(ROOT / "include"), str(PKG / "tune" / "seg_autotune.cu"), "-o", str(out)]
-    subprocess.run(cmd, check=True)
-    return out
+    outs, procs = [], []
+    for dt in range(4):
+        out = PKG / "_build" / f"seg_autotune_{dt}"
+        cmd = [nvcc, "-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "--expt-extended-lambda",
+               f"-DPP_TUNE_DT={dt}", "-I", str(PKG / "csrc"), "-I", str(ROOT / "include"),
+               str(PKG / "tune" / "seg_autotune.cu"), "-o", str(out)]
+        procs.append(subprocess.Popen(cmd))
+        outs.append(out)
+    for p in procs:
+        if p.wait() != 0:
+            raise RuntimeError("compiling the segmented-scan autotuner failed")
+    return outs
 
 
-def run(exe: Path) -> list[dict]:
-    r = subprocess.run([str(exe)], capture_output=True, text=True, check=True, timeout=2400)
+def run(exes: list[Path]) -> list[dict]:
     rows = []
-    for line in r.stdout.splitlines():
-        line = line.strip()
-        if line.startswith("{"):
-            rows.append(json.loads(line))
+    for exe in exes:
+        r = subprocess.run([str(exe)], capture_output=True, text=True, check=True, timeout=2400)
+        for line in r.stdout.splitlines():
+            line = line.strip()
+            if line.startswith("{"):
+                rows.append(json.loads(line))
     return rows
 
 
@@ -89,9 +99,9 @@ def write_inc(choice: dict, device: str) -> Path:
 
 
 def main() -> None:
-    exe = compile_tuner()
+    exes = compile_tuners()
     t0 = time.time()
-    rows = run(exe)
+    rows = run(exes)
     choice = choose(rows)
     try:
         device = subprocess.run(["nvidia-smi", "--query-gpu=name", "--format=csv,noheader"], capture_output=True,

@@ -1,19 +1,20 @@
 // Autotuner of the batched segmented scan: times every variant of the
-// segmented kernel on two length distributions and four payload types and
+// segmented kernel on two length distributions and one payload type (chosen
+// at compile time with -DPP_TUNE_DT=0..3: int32, float32, int64, float64) and
 // prints one JSON line per (payload, distribution, variant). Variants:
-//   striped chunks (LAY 0): compute warps {8, 16} (block size 256 / 512
-//     compute threads), items per thread {8, 16, 32}, chunk vector width
-//     {8, 16} bytes;
-//   lane rows (LAY 2): compute warps {12, 14, 16}, {5, 7, 9} 16-byte chunks
-//     per lane (items per thread 20 / 28 / 36 for 4-byte payloads).
+//   striped chunks (LAY 0): compute warps {4, 8, 16} (block size 128 / 256 /
+//     512 compute threads), items per thread {4, 8, 16, 32}, chunk vector
+//     width {8, 16} bytes;
+//   lane rows (LAY 2): compute warps {12, 14, 16, 18, 20}, {5, 7, 9} 16-byte
+//     chunks per lane (items per thread 20 / 28 / 36 for 4-byte payloads).
 // Distributions: "long" = 65,536 segments with lengths floor(exp(U[0, ln 2^16]))
 // clipped to [1, 2^16] (about 2^28 elements, the batched benchmark), "short" =
 // 2^21 segments with lengths U[1, 128] (about 2^27 elements). Payloads: int32
 // U[0,1000), float32 N(0,1), int64 U[0,1000), float64 N(0,1). Every variant's
 // output is checked against the first (default) variant of the same case.
-// ppautotune.py compiles and runs it, and writes the variant with the best
-// worst-case throughput per (payload size, distribution) to
-// csrc/pp/seg_tuned.inc.
+// ppautotune.py compiles one binary per payload (in parallel), runs them, and
+// writes the variant with the best worst-case throughput per (payload size,
+// distribution) to csrc/pp/seg_tuned.inc.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -133,10 +134,11 @@ void run_variant(Workload<T>& w, const char* dt, bool is_reference) {
   }
 }
 
-// striped: items per thread {8, 16, 32} at vector widths {8, 16} bytes
+// striped: items per thread {4, 8, 16, 32} at vector widths {8, 16} bytes
 template <class T, int NC, int VB>
 void run_striped_vb(Workload<T>& w, const char* dt) {
   constexpr int V = VB / int(sizeof(T));
+  if constexpr (4 / V >= 1) run_variant<T, 0, NC, 4 / V, VB>(w, dt, false);
   run_variant<T, 0, NC, 8 / V, VB>(w, dt, false);
   run_variant<T, 0, NC, 16 / V, VB>(w, dt, false);
   run_variant<T, 0, NC, 32 / V, VB>(w, dt, false);
@@ -172,11 +174,14 @@ void tune(const char* dt, const char* dist, const std::vector<int64_t>& off) {
   w.ctrl_bytes = workspace_bytes_for_desc_words((w.n / 128 + 1) * 2);
   cudaMalloc(&w.ctrl, w.ctrl_bytes);
   run_variant<T, 0, 16, 8, 16>(w, dt, true);  // default variant (16 warps, 8 16-byte chunks): reference output
+  run_striped<T, 4>(w, dt);
   run_striped<T, 8>(w, dt);
   run_striped<T, 16>(w, dt);
   run_rows<T, 12>(w, dt);
   run_rows<T, 14>(w, dt);
   run_rows<T, 16>(w, dt);
+  run_rows<T, 18>(w, dt);
+  run_rows<T, 20>(w, dt);
   cudaFree(w.in);
   cudaFree(w.out);
   cudaFree(w.ref);
@@ -201,14 +206,24 @@ int main() {
   for (int s = 0; s < SS; ++s) sht[s + 1] = sht[s] + us(rng);
   printf("{\"long_segments\":%d,\"long_elements\":%lld,\"short_segments\":%d,\"short_elements\":%lld}\n", SL,
          (long long)lng.back(), SS, (long long)sht.back());
-  tune<int32_t>("i32", "long", lng);
-  tune<float>("f32", "long", lng);
-  tune<int64_t>("i64", "long", lng);
-  tune<double>("f64", "long", lng);
-  tune<int32_t>("i32", "short", sht);
-  tune<float>("f32", "short", sht);
-  tune<int64_t>("i64", "short", sht);
-  tune<double>("f64", "short", sht);
+#ifndef PP_TUNE_DT
+#define PP_TUNE_DT 0
+#endif
+#if PP_TUNE_DT == 0
+  using T = int32_t;
+  const char* dt = "i32";
+#elif PP_TUNE_DT == 1
+  using T = float;
+  const char* dt = "f32";
+#elif PP_TUNE_DT == 2
+  using T = int64_t;
+  const char* dt = "i64";
+#else
+  using T = double;
+  const char* dt = "f64";
+#endif
+  tune<T>(dt, "long", lng);
+  tune<T>(dt, "short", sht);
   printf("{\"last_error\":\"%s\"}\n", cudaGetErrorString(cudaGetLastError()));
   return 0;
 }
