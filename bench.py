@@ -199,8 +199,8 @@ def run_ours(args) -> dict | None:
     # sanity: last prefix == total (mod 2^32), first == in[0]
     total = int(d_in.sum(dtype=torch.int64).item()) & 0xFFFFFFFF  # no converted copy of the input
     verified = (int(d_out[-1].item()) & 0xFFFFFFFF) == total and int(d_out[0].item()) == int(d_in[0].item())
-    # hand torch's scratch of that check back to the driver: a large cached but unused block slowed the timed
-    # scans by ~3% on GB300
+    # free torch's cached scratch of that check (a large cached but unused block slowed the timed scans by ~3%
+    # on GB300)
     torch.cuda.empty_cache()
 
     vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0]
@@ -249,6 +249,7 @@ def run_ours(args) -> dict | None:
     e2e_s = max_over_ranks(torch, time.perf_counter() - t0)
     e2e_value = ws * algo_bytes * e2e_steps / e2e_s / 1e9
     e2e_ok = (int(h_out[-1]) & 0xFFFFFFFF) == total and int(h_out[0]) == int(h_in[0])
+    link = host_link_rates(torch, h_in, h_out, d_in, d_out)
     del h_in, h_out
 
     secondary = {} if args.no_secondary else run_secondary(torch, pp, stream, args, d_in, d_out)
@@ -299,12 +300,43 @@ def run_ours(args) -> dict | None:
             "d2h_bytes_per_step": n * 4,
             "api": "pp_decoupled_scan_host (pinned host buffers; streamed in 64 MiB chunks, both copy directions overlapping the scans)",
             "verified_tail": e2e_ok,
+            "host_link_gbs_this_run": link,
         },
         "gpu_launches": args.steps,
         "clocks": clocks,
         "cpu_baseline": cpu,
         "secondary": secondary,
     }
+
+
+def host_link_rates(torch, h_in, h_out, d_in, d_out) -> dict:
+    """Plain pinned copies of the same arrays in this run (GB/s): host to device, device to host, and both at once
+    on two streams (bytes of both directions counted) -- the bound of the end-to-end figure."""
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    nbytes = h_in.numel() * h_in.element_size()
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    def h2d():
+        with torch.cuda.stream(s1):
+            d_in.copy_(h_in, non_blocking=True)
+
+    def d2h():
+        with torch.cuda.stream(s2):
+            h_out.copy_(d_out, non_blocking=True)
+
+    def both():
+        h2d()
+        d2h()
+
+    return {"h2d": round(nbytes / timed(h2d) / 1e9, 1), "d2h": round(nbytes / timed(d2h) / 1e9, 1),
+            "both_directions": round(2 * nbytes / timed(both) / 1e9, 1)}
 
 
 def run_secondary(torch, pp, stream, args, d_in32, d_out32) -> dict:
@@ -332,10 +364,11 @@ def run_secondary(torch, pp, stream, args, d_in32, d_out32) -> dict:
     # flush itself lands in the timed launch
     flush = torch.zeros(1 << 26, dtype=torch.int32, device="cuda")
 
-    def flushed_rate(fn, nbytes, reps=10):
+    def flushed_rate(fn, nbytes, reps=21):
+        # median of `reps` launches, each timed on its own after the flush
         for _ in range(3):
             fn()
-        total = 0.0
+        times = []
         for _ in range(reps):
             flush.sum()
             a = torch.cuda.Event(enable_timing=True)
@@ -344,16 +377,19 @@ def run_secondary(torch, pp, stream, args, d_in32, d_out32) -> dict:
             fn()
             b.record(stream)
             b.synchronize()
-            total += a.elapsed_time(b)
+            times.append(a.elapsed_time(b))
         if pp.stream_status(sh) != 0:
             raise RuntimeError("device error in the 2^24 benchmark")
-        return round(nbytes * reps / (total * 1e-3) / 1e9, 2)
+        ms = sorted(times)[len(times) // 2]
+        return round(nbytes / (ms * 1e-3) / 1e9, 2)
 
     out["u32_inclusive_plus_2p24_l2_flushed"] = flushed_rate(
         lambda: pp.decoupled_scan_device("inclusive", "plus", x24.data_ptr(), y24.data_ptr(), n24, "u32", stream=sh),
         8 * n24)
     out["u32_sum_reduce_2p24_l2_flushed"] = flushed_rate(
         lambda: pp.reduce("plus", x24.data_ptr(), n24, "u32", r24.data_ptr(), stream=sh), 4 * n24)
+    # the same protocol on a device copy of the same 64 MiB: what "copy speed" is at this size
+    out["device_copy_64mib_l2_flushed"] = flushed_rate(lambda: y24.copy_(x24), 8 * n24)
     del x24, y24, flush
 
     out["u32_exclusive_plus_2p30"] = rate(
