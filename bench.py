@@ -543,7 +543,12 @@ def bench_segmented(torch, pp, stream, steps) -> dict:
 
 def bench_cumsum(torch, stream, steps) -> dict:
     """Differentiable cumsum of a 4096 x 8192 f32 N(0,1) tensor through the
-    libtorch binding: forward + backward GB/s (2 * B * L * 4 bytes each)."""
+    libtorch binding: forward + backward GB/s (2 * B * L * 4 bytes each).
+
+    The headline figure replays the whole step (forward, backward, gradient
+    accumulation) as one CUDA graph; an eager step is bound by the host (the
+    autograd engine's bookkeeping takes longer than the two scans), so it is
+    reported beside it, with torch.cumsum's graph-replayed step for scale."""
     try:
         import ppcumsum
 
@@ -553,16 +558,43 @@ def bench_cumsum(torch, stream, steps) -> dict:
     g = torch.Generator(device="cuda").manual_seed(5)
     x = torch.randn(4096, 8192, device="cuda", generator=g).requires_grad_(True)
     up = torch.randn(4096, 8192, device="cuda", generator=g)
+    nbytes = 2 * (2 * 4096 * 8192 * 4)
+    cur = torch.cuda.current_stream()
 
     def step():
         x.grad = None
         ext.cumsum(x).backward(up)
 
-    ms, _ = time_device(torch, step, steps, 2, torch.cuda.current_stream())
-    nbytes = 2 * (2 * 4096 * 8192 * 4)
+    def torch_step():
+        x.grad = None
+        torch.cumsum(x, 1).backward(up)
+
+    def graphed(fn):
+        side = torch.cuda.Stream()
+        side.wait_stream(cur)
+        with torch.cuda.stream(side):
+            for _ in range(3):
+                fn()
+        cur.wait_stream(side)
+        gr = torch.cuda.CUDAGraph()
+        x.grad = None
+        with torch.cuda.graph(gr):
+            fn()
+        return gr
+
+    eager_ms, _ = time_device(torch, step, steps, 2, cur)
+    gr = graphed(step)
+    graph_ms, _ = time_device(torch, gr.replay, steps, 2, cur)
     ref = torch.flip(torch.cumsum(torch.flip(up.double(), [1]), 1), [1])
-    return {"fwd_bwd_gbs": round(nbytes * steps / (ms * 1e-3) / 1e9, 2), "ms_per_fwd_bwd": round(ms / steps, 4),
-            "grad_max_abs_err": float((x.grad.double() - ref).abs().max())}
+    err = float((x.grad.double() - ref).abs().max())
+    del gr
+    tgr = graphed(torch_step)
+    torch_ms, _ = time_device(torch, tgr.replay, steps, 2, cur)
+    del tgr
+    rate = lambda ms: round(nbytes * steps / (ms * 1e-3) / 1e9, 2)
+    return {"fwd_bwd_gbs": rate(graph_ms), "ms_per_fwd_bwd": round(graph_ms / steps, 4), "step": "one CUDA graph replay",
+            "eager_fwd_bwd_gbs": rate(eager_ms), "eager_ms_per_fwd_bwd": round(eager_ms / steps, 4),
+            "torch_cumsum_fwd_bwd_gbs_graph": rate(torch_ms), "grad_max_abs_err": err}
 
 
 # ---------------------------------------------------------------------------------
