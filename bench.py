@@ -242,11 +242,14 @@ def run_ours(args) -> dict | None:
     e2e_step()
     barrier(torch)
     t0 = time.perf_counter()
+    step_ends = []
     for _ in range(e2e_steps):
-        e2e_step()
+        e2e_step()  # returns once the results are in the host buffer
+        step_ends.append(time.perf_counter())
     torch.cuda.synchronize()
     barrier(torch)
     e2e_s = max_over_ranks(torch, time.perf_counter() - t0)
+    e2e_step_ms = [round((b - a) * 1e3, 2) for a, b in zip([t0] + step_ends[:-1], step_ends)]
     e2e_value = ws * algo_bytes * e2e_steps / e2e_s / 1e9
     e2e_ok = (int(h_out[-1]) & 0xFFFFFFFF) == total and int(h_out[0]) == int(h_in[0])
     link = host_link_rates(torch, h_in, h_out, d_in, d_out)
@@ -301,6 +304,7 @@ def run_ours(args) -> dict | None:
             "api": "pp_decoupled_scan_host (pinned host buffers; streamed in 64 MiB chunks, both copy directions overlapping the scans)",
             "verified_tail": e2e_ok,
             "host_link_gbs_this_run": link,
+            "step_ms": e2e_step_ms,
         },
         "gpu_launches": args.steps,
         "clocks": clocks,
