@@ -133,7 +133,8 @@ def barrier(torch):
 
 def max_over_ranks(torch, v: float) -> float:
     if torch.distributed.is_available() and torch.distributed.is_initialized():
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dev = "cuda" if torch.distributed.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         return float(t.item())
     return v
