@@ -475,28 +475,34 @@ inline Status reduce(cudaStream_t s, const T* in, uint64_t n, T* d_result, void*
 
 // ---------------------------------------------------------------------------
 // Batched segmented scan / reduce and row scans (segmented.cuh).
-// Variant of the segmented kernel: 4-byte elements take the autotuned one
-// (seg_tuned.inc, written by ppautotune.py), others 16 warps x 16-byte chunks.
 #include "seg_tuned.inc"
 // Variant of the segmented kernel. CSR forward scans and reductions take the
-// autotuned variant of their payload size and segment-length class (mean
-// length n / S >= kSegLongMean: "long"); row scans that fall back to this
-// kernel (uniform heads, either direction) take 16 warps of 8 16-byte chunks.
+// autotuned variant (seg_tuned.inc, written by ppautotune.py) of their payload
+// type and segment-length class (mean length n / S >= kSegLongMean: "long");
+// unsigned payloads take their signed counterpart's. Row scans that fall back
+// to this kernel (uniform heads, either direction) take 16 warps of 8 16-byte
+// chunks.
 constexpr uint64_t kSegLongMean = 512;
-template <int LAY_, int NC_, int CH_, int VB_, class T>
+template <int LAY_, int NC_, int CH_, int VB_, class T, int LBW_ = 4>
 struct SegVariant {
-  static constexpr int LAY = LAY_, NC = NC_, CH = CH_, VB = VB_, LBW = 4;
+  static constexpr int LAY = LAY_, NC = NC_, CH = CH_, VB = VB_, LBW = LBW_;
   static constexpr int TILE_BYTES = NC * 32 * CH * VB;
   static constexpr int ST0 = 196608 / TILE_BYTES;
   static constexpr int STAGES = LAY == 2 ? 3 : (ST0 < 2 ? 2 : (ST0 > 8 ? 8 : ST0));
 };
+#define PP_SEG_VARIANT(DT, LEN)                                                                              \
+  SegVariant<PP_SEG_##DT##_##LEN##_LAY, PP_SEG_##DT##_##LEN##_NC, PP_SEG_##DT##_##LEN##_CH, PP_SEG_##DT##_##LEN##_VB, \
+             T, PP_SEG_##DT##_##LEN##_LBW>
 template <class T, bool LONG>
 using SegTunedCsr = std::conditional_t<
-    sizeof(T) == 4,
-    std::conditional_t<LONG, SegVariant<PP_SEG_4B_LONG_LAY, PP_SEG_4B_LONG_NC, PP_SEG_4B_LONG_CH, PP_SEG_4B_LONG_VB, T>,
-                       SegVariant<PP_SEG_4B_SHORT_LAY, PP_SEG_4B_SHORT_NC, PP_SEG_4B_SHORT_CH, PP_SEG_4B_SHORT_VB, T>>,
-    std::conditional_t<LONG, SegVariant<PP_SEG_8B_LONG_LAY, PP_SEG_8B_LONG_NC, PP_SEG_8B_LONG_CH, PP_SEG_8B_LONG_VB, T>,
-                       SegVariant<PP_SEG_8B_SHORT_LAY, PP_SEG_8B_SHORT_NC, PP_SEG_8B_SHORT_CH, PP_SEG_8B_SHORT_VB, T>>>;
+    std::is_floating_point_v<T>,
+    std::conditional_t<sizeof(T) == 4,
+                       std::conditional_t<LONG, PP_SEG_VARIANT(F32, LONG), PP_SEG_VARIANT(F32, SHORT)>,
+                       std::conditional_t<LONG, PP_SEG_VARIANT(F64, LONG), PP_SEG_VARIANT(F64, SHORT)>>,
+    std::conditional_t<sizeof(T) == 4,
+                       std::conditional_t<LONG, PP_SEG_VARIANT(I32, LONG), PP_SEG_VARIANT(I32, SHORT)>,
+                       std::conditional_t<LONG, PP_SEG_VARIANT(I64, LONG), PP_SEG_VARIANT(I64, SHORT)>>>;
+#undef PP_SEG_VARIANT
 template <class T>
 using SegUniform = SegVariant<0, 16, 8, 16, T>;
 template <class Tn, class T, class Op>

@@ -4,16 +4,17 @@ Compiles tune/seg_autotune.cu once per payload type, in parallel (variants of
 the segmented kernel: striped chunks over compute warps {4, 8, 16} = block size
 {128, 256, 512} threads, items per thread {4, 8, 16, 32} and chunk vector width
 {8, 16} bytes; lane rows over {12, 14, 16, 18, 20} warps with {5, 7, 9} 16-byte
-chunks per lane), runs the binaries one after another on the GPU
-on two length distributions ("long": 65,536 log-uniform segments in [1, 2^16];
-"short": 2^21 segments of U[1, 128]) with int32, float32, int64 and float64
-payloads, records every measurement in tune/seg_autotune_results.json and
-writes, per payload size (4 / 8 bytes) and distribution, the variant with the
-best worst-case throughput over that size's two payloads to
+chunks per lane and look-back polls of {1, 4} windows), runs the binaries one
+after another on the GPU on two length distributions ("long": 65,536
+log-uniform segments in [1, 2^16]; "short": 2^21 segments of U[1, 128]) with
+int32, float32, int64 and float64 payloads, records every measurement in tune/seg_autotune_results.json and
+writes, per payload type and distribution, the fastest variant to
 csrc/pp/seg_tuned.inc. The library's CSR segmented launches pick the long or
-short variant from the mean segment length.
+short variant from the mean segment length; unsigned payloads take the variant
+of the signed type of their size.
 
-    python sycl-building-blocks_gb300/ppautotune.py
+    python sycl-building-blocks_gb300/ppautotune.py                  # measure and choose
+    python sycl-building-blocks_gb300/ppautotune.py --from-results   # choose again from the saved run
 """
 
 from __future__ import annotations
@@ -58,59 +59,55 @@ def run(exes: list[Path]) -> list[dict]:
     return rows
 
 
-SIZES = {"i32": 4, "f32": 4, "i64": 8, "f64": 8}
+DTYPES = ("i32", "f32", "i64", "f64")
 
 
 def choose(rows: list[dict]) -> dict:
-    """Best worst-case variant per (payload size, distribution)."""
+    """Fastest variant per (payload type, distribution)."""
     ok = [r for r in rows if "ms" in r and r.get("err") == 0 and r.get("matches_default")]
     out = {}
-    for size in (4, 8):
+    for dt in DTYPES:
         for dist in ("long", "short"):
-            by_key: dict[tuple, dict] = {}
-            for r in ok:
-                if SIZES[r["dtype"]] == size and r["dist"] == dist:
-                    by_key.setdefault((r["lay"], r["nc"], r["ch"], r["vb"]), {})[r["dtype"]] = r
-            best, best_score = None, -1.0
-            for key, d in by_key.items():
-                if len(d) < 2:
-                    continue
-                score = min(v["elems_per_s"] for v in d.values())
-                if score > best_score:
-                    best, best_score = key, score
-            if best is None:
-                raise RuntimeError(f"no valid variant for {size}-byte payloads, {dist} segments")
-            out[f"{size}B_{dist}"] = {"lay": best[0], "nc": best[1], "ch": best[2], "vb": best[3],
-                                      "worst_case_elems_per_s": best_score}
+            cand = [r for r in ok if r["dtype"] == dt and r["dist"] == dist]
+            if not cand:
+                raise RuntimeError(f"no valid variant for {dt} payloads, {dist} segments")
+            b = max(cand, key=lambda r: r["elems_per_s"])
+            out[f"{dt}_{dist}"] = {"lay": b["lay"], "nc": b["nc"], "ch": b["ch"], "vb": b["vb"],
+                                   "lbw": b.get("lbw", 4), "elems_per_s": b["elems_per_s"]}
     return out
 
 
 def write_inc(choice: dict, device: str) -> Path:
     inc = PKG / "csrc" / "pp" / "seg_tuned.inc"
-    lines = ["// Generated by ppautotune.py: segmented-scan variants with the best worst-case",
-             f"// throughput per payload size and segment-length class on {device}",
+    lines = ["// Generated by ppautotune.py: the fastest segmented-scan variant per payload",
+             f"// type and segment-length class on {device}",
              "// (see tune/seg_autotune_results.json)."]
     for key, c in choice.items():
-        size, dist = key.split("_")
-        for f in ("lay", "nc", "ch", "vb"):
-            lines.append(f"#define PP_SEG_{size}_{dist.upper()}_{f.upper()} {c[f]}")
+        dt, dist = key.split("_")
+        for f in ("lay", "nc", "ch", "vb", "lbw"):
+            lines.append(f"#define PP_SEG_{dt.upper()}_{dist.upper()}_{f.upper()} {c[f]}")
     inc.write_text("\n".join(lines) + "\n")
     return inc
 
 
 def main() -> None:
-    exes = compile_tuners()
-    t0 = time.time()
-    rows = run(exes)
+    results = PKG / "tune" / "seg_autotune_results.json"
+    if "--from-results" in sys.argv:  # choose again from the committed measurements, no GPU needed
+        saved = json.loads(results.read_text())
+        rows, device, seconds = saved["rows"], saved["device"], saved["seconds"]
+    else:
+        exes = compile_tuners()
+        t0 = time.time()
+        rows = run(exes)
+        seconds = round(time.time() - t0, 1)
+        try:
+            device = subprocess.run(["nvidia-smi", "--query-gpu=name", "--format=csv,noheader"], capture_output=True,
+                                    text=True).stdout.strip().splitlines()[0]
+        except Exception:
+            device = "unknown GPU"
     choice = choose(rows)
-    try:
-        device = subprocess.run(["nvidia-smi", "--query-gpu=name", "--format=csv,noheader"], capture_output=True,
-                                text=True).stdout.strip().splitlines()[0]
-    except Exception:
-        device = "unknown GPU"
-    (PKG / "tune" / "seg_autotune_results.json").write_text(
-        json.dumps({"device": device, "seconds": round(time.time() - t0, 1), "choice": choice, "rows": rows},
-                   indent=1) + "\n")
+    results.write_text(json.dumps({"device": device, "seconds": seconds, "choice": choice, "rows": rows},
+                                  indent=1) + "\n")
     print(write_inc(choice, device), choice)
 
 
