@@ -242,21 +242,22 @@ struct pol_commutative<F64CarryF32> : std::true_type {};
 // LAY selects the layout of the passes over a tile:
 //   0 striped: chunk c of a warp's segment is 32 consecutive 16-byte chunks,
 //     one per lane; every chunk needs its own warp scan;
-//   1 lane-blocked: each lane owns a row of CH consecutive chunks; one warp
-//     scan per segment, chunk prefixes inside the row;
-//   2 rows: as 1, and the reduce pass leaves each row's total in shared
-//     memory, so the scan pass is one thread-serial chain along the row
-//     (Pol::row_incl / row_excl: one combine per element).
-// CH odd in layouts 1 and 2: rows of CH * 16 bytes then start in 8 different
+//   2 rows: each lane owns a row of CH consecutive chunks; the reduce pass
+//     walks the row in order and leaves the row's prefix inside its segment
+//     in shared memory, so the scan pass is one thread-serial chain along the
+//     row (Pol::row_incl / row_excl: one combine per element).
+// CH odd in the rows layout: rows of CH * 16 bytes then start in 8 different
 // 16-byte bank groups for any 8 consecutive lanes, so row reads are free of
-// bank conflicts; results go back into the row and leave striped.
-template <class Pol, int NC_, int CH_, int STAGES_, int LBW_, int LAY_ = 0, int NR_ = 0, int SW_ = 0>
+// bank conflicts; results go back into the row and leave striped or by bulk
+// copy.
+template <class Pol, int NC_, int CH_, int STAGES_, int LBW_, int LAY_ = 0, int SW_ = 0>
 struct StagedCfg {
   using in_t = typename Pol::in_t;
   using acc_t = typename Pol::acc_t;
   using carry_t = typename Pol::carry_t;
   static constexpr int LAY = LAY_;
-  static_assert(LAY_ == 0 || (CH_ % 2) == 1, "lane rows need an odd chunk count");
+  static_assert(LAY_ == 0 || LAY_ == 2, "striped (0) or rows (2) layout");
+  static_assert(LAY_ == 0 || (CH_ % 2) == 1, "rows need an odd chunk count");
   static constexpr int NC = NC_;            // compute warps
   static constexpr int CH = CH_;            // 16-byte chunks per lane per segment
   static constexpr int STAGES = STAGES_;    // shared-memory ring depth
@@ -266,9 +267,8 @@ struct StagedCfg {
   static constexpr int SEG = 32 * CH * V;   // elements per compute warp
   static constexpr int TILE = NC * SEG;
   static constexpr int TILE_BYTES = TILE * int(sizeof(in_t));
-  static constexpr int NR = NR_;            // reducer warps (0: the compute warps reduce too)
   static constexpr int SW = SW_;            // store warps (1: a warp writes finished tiles back by bulk copy)
-  static constexpr int THREADS = (NC + NR + 2 + SW) * 32;
+  static constexpr int THREADS = (NC + 2 + SW) * 32;
   // per-stage metadata
   static constexpr size_t META_AGG = 0;  // acc_t[NC] segment aggregates, then their exclusive prefixes
   static constexpr size_t META_PREF = align_up(NC * sizeof(acc_t), 16);   // carry_t tile exclusive prefix
@@ -278,8 +278,8 @@ struct StagedCfg {
   static constexpr size_t META_ROWS = align_up(META_CNT + 4, 16);  // acc_t[NC*32] row prefixes in the segment
   static constexpr size_t META_BYTES = align_up(META_ROWS + (LAY_ == 2 ? NC_ * 32 * sizeof(acc_t) : 0), 16);
   static constexpr size_t OFF_META = size_t(STAGES) * TILE_BYTES;
-  static constexpr size_t OFF_BAR = align_up(OFF_META + STAGES * META_BYTES, 8);  // 6 barriers / stage
-  static constexpr size_t SMEM = OFF_BAR + 6 * STAGES * 8;
+  static constexpr size_t OFF_BAR = align_up(OFF_META + STAGES * META_BYTES, 8);  // 5 barriers / stage
+  static constexpr size_t SMEM = OFF_BAR + 5 * STAGES * 8;
 };
 
 // Geometry of tile t in the staged kernel. The tile grid is shifted by `head`
@@ -529,33 +529,26 @@ __device__ __forceinline__ bool lookback_pipelined(const Pol& pol, const uint64_
   return true;
 }
 
-// NR: 0 = every compute warp runs the reduce pass of tile k+1 before the scan
-// pass of tile k; > 0 = NR dedicated reducer warps reduce tiles as soon as
-// they arrive (up to STAGES-1 ahead of the scan), so a late prefix never
-// delays the publication of the next aggregates.
+// Every compute warp runs the reduce pass of tile k+1 before the scan pass of
+// tile k, so the next aggregate is published before this CTA waits for a
+// prefix.
 // PG: 0 = one look-back poll in flight; > 0 = two, the second PG ns later.
-// BS: 1 = in the row layouts each compute warp writes its finished segment
-// back with one bulk copy (shared -> global) instead of striped stores;
-// 2 = one extra store warp writes each finished tile back with one bulk copy
-// and frees the stage, so the compute warps never wait for stores.
-// LA: how many tiles the compute warps reduce ahead of the one they scan (the
-// look-back of a tile has LA reduce passes and LA - 1 scan passes to finish);
-// needs STAGES >= LA + 2 to keep a load in flight.
-// EXC: -1 = scan kind read from the arguments; 0 / 1 = inclusive / exclusive
-// compiled in (one code path: smaller kernels for the instruction cache).
+// BS: 0 = the compute warps store their results; 2 = one extra store warp
+// writes each finished tile of the rows layout back with one bulk copy and
+// frees the stage, so the compute warps never wait for stores.
 // TK: when the producer draws the ticket of the next tile for a stage.
 //   0: right after issuing the previous copy (a full stage life ahead);
-//   1: when the compute warps start scanning the tile still in that stage;
 //   2: once the stage is free.
 // Later tickets make the order of tickets follow the order in which tiles
 // reach their reduce pass more closely, so predecessors' aggregates arrive
 // closer together; earlier ones hide the latency of the ticket atomic.
-template <class Pol, int NC, int CH, int STAGES, int LBW, int LAY = 0, int TK = 0, int NR = 0,
-          unsigned PG = 0, int EXC = -1, int BS = 0, int LA = 1, class Trace = NoTrace>
-__global__ void __launch_bounds__((NC + NR + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
+template <class Pol, int NC, int CH, int STAGES, int LBW, int LAY = 0, int TK = 0, unsigned PG = 0, int BS = 0,
+          class Trace = NoTrace>
+__global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
     decoupled_staged_kernel(const ScanArgs args) {
-  using Cfg = StagedCfg<Pol, NC, CH, STAGES, LBW, LAY, NR, (BS == 2 ? 1 : 0)>;
-  static_assert(BS != 2 || (LAY >= 1 && NR == 0), "the store warp serves the row layouts");
+  using Cfg = StagedCfg<Pol, NC, CH, STAGES, LBW, LAY, (BS == 2 ? 1 : 0)>;
+  static_assert(TK == 0 || TK == 2, "tickets a stage life ahead (0) or once the stage is free (2)");
+  static_assert(BS == 0 || (BS == 2 && LAY == 2), "the store warp serves the rows layout");
   using in_t = typename Pol::in_t;
   using out_t = typename Pol::out_t;
   using acc_t = typename Pol::acc_t;
@@ -572,8 +565,7 @@ __global__ void __launch_bounds__((NC + NR + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
   uint64_t* empty = bars + STAGES;
   uint64_t* aggb = bars + 2 * STAGES;
   uint64_t* prefb = bars + 3 * STAGES;
-  uint64_t* sgo = bars + 4 * STAGES;      // compute warp 0 starts the scan pass (TK == 1)
-  uint64_t* scanned = bars + 5 * STAGES;  // the compute warps' results are in the stage (BS == 2)
+  uint64_t* scanned = bars + 4 * STAGES;  // the compute warps' results are in the stage (BS == 2)
   auto meta = [&](int s) { return smem + Cfg::OFF_META + size_t(s) * Cfg::META_BYTES; };
   auto s_aggs = [&](int s) { return reinterpret_cast<acc_t*>(meta(s) + Cfg::META_AGG); };
   auto s_pref = [&](int s) { return reinterpret_cast<carry_t*>(meta(s) + Cfg::META_PREF); };
@@ -601,9 +593,8 @@ __global__ void __launch_bounds__((NC + NR + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
       ptx::mbar_init(&full[s], 1);
       ptx::mbar_init(&empty[s], BS == 2 ? 1 : NC);
       ptx::mbar_init(&scanned[s], NC);
-      ptx::mbar_init(&aggb[s], NR > 0 ? NR : NC);
+      ptx::mbar_init(&aggb[s], NC);
       ptx::mbar_init(&prefb[s], 1);
-      ptx::mbar_init(&sgo[s], 1);
       *s_cnt(s) = 0u;
     }
     ptx::fence_mbar_init();
@@ -627,10 +618,6 @@ __global__ void __launch_bounds__((NC + NR + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
         const int s = k % STAGES;
         if (k >= STAGES) {
           const uint32_t par = ((k / STAGES) - 1) & 1;
-          if constexpr (TK == 1) {
-            if (!mbar_wait_bounded(&sgo[s], par, hdr, tmo, 0ull)) break;
-            t = draw();
-          }
           if (!mbar_wait_bounded(&empty[s], par, hdr, tmo, (unsigned long long)t)) break;
           if constexpr (TK == 2) t = draw();
           pending &= ~(1u << s);
@@ -702,7 +689,7 @@ __global__ void __launch_bounds__((NC + NR + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
       }
       __syncwarp();
     }
-  } else if (BS == 2 && warp == NC + NR + 2) {
+  } else if (BS == 2 && warp == NC + 2) {
     // ------------------------------------------------------------ store
     // Each finished full tile leaves as one bulk copy; the stage is freed as
     // soon as the copy has read it. Partial tiles and outputs that are not
@@ -730,12 +717,10 @@ __global__ void __launch_bounds__((NC + NR + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
     }
   } else {
     // ------------------------------------------------------------ compute
-    // split mode: warps 2..NR+1 reduce, the NC warps after them scan
-    const bool reducer = NR > 0 && warp < 2 + NR;
-    const int w = NR > 0 ? (reducer ? warp - 2 : warp - 2 - NR) : warp - 2;
+    const int w = warp - 2;
     const in_t* gin = static_cast<const in_t*>(args.in);
     out_t* gout = static_cast<out_t*>(args.out);
-    const bool excl_kind = EXC >= 0 ? EXC == 1 : args.exclusive != 0;
+    const bool excl_kind = args.exclusive != 0;
     auto aop = [&](const acc_t& x, const acc_t& y) { return pol.aop(x, y); };
 
     const bool out_vec = ((reinterpret_cast<uintptr_t>(gout) - uintptr_t(head) * sizeof(out_t)) & 15u) == 0;
@@ -787,24 +772,13 @@ __global__ void __launch_bounds__((NC + NR + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
       load_at(s, seg * Cfg::SEG + (c * 32 + lane) * V, g, a);
     };
     // Writes this warp's finished segment (already in the stage, in order):
-    // one bulk copy when the whole segment is valid and the output aligned,
-    // else striped 16-byte stores. Returns once the stage may be reused.
+    // with a store warp, a full tile with an aligned output leaves by its bulk
+    // copy; else striped 16-byte stores. Returns once the stage may be reused.
     auto store_segment = [&](const unsigned char* stage, const StagedGeom& g) {
       const int s0 = w * Cfg::SEG;
       if (BS == 2 && out_vec && g.lo == 0 && g.valid == TILE) {
         // the store warp writes the whole tile once every segment is in
         ptx::fence_proxy_async_smem();
-        return;
-      }
-      if (BS == 1 && out_vec && s0 >= g.lo && s0 + Cfg::SEG <= g.valid) {
-        ptx::fence_proxy_async_smem();
-        __syncwarp();
-        if (lane == 0) {
-          ptx::bulk_s2g_hint(gout + (g.gbase + s0), stage + size_t(s0) * sizeof(in_t),
-                             uint32_t(Cfg::SEG * sizeof(out_t)), ptx::policy_evict_first());
-          ptx::bulk_commit();
-          ptx::bulk_wait_read<0>();
-        }
         return;
       }
       __syncwarp();
@@ -914,51 +888,21 @@ __global__ void __launch_bounds__((NC + NR + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
         trace_now(kTrRGot, tile);
       }
       const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(tile, n, head);
-      if constexpr (NR > 0) {
-        for (int seg = w; seg < NC; seg += NR) record_segment(s, seg, tile, reduce_segment(s, seg, g));
-      } else {
-        record_segment(s, w, tile, reduce_segment(s, w, g));
-      }
+      record_segment(s, w, tile, reduce_segment(s, w, g));
       if (lane == 0) ptx::mbar_arrive(&aggb[s]);
       __syncwarp();
       return true;
     };
 
-    if (reducer) {
-      for (int k = 0; reduce_pass(k); ++k) {
-      }
-    }
-    static_assert(LA >= 1 && (LA == 1 || STAGES >= LA + 2), "reduce-ahead needs LA + 2 stages");
-    // reduce passes run LA tiles ahead of scan passes: nred tiles reduced so far
-    int nred = 0;
-    bool more = true;
-    if constexpr (NR == 0) {
-      while (more && nred < LA) {
-        more = reduce_pass(nred);
-        if (more) ++nred;
-      }
-    }
-    bool have = NR > 0 ? !reducer : nred > 0;
+    // the reduce pass runs one tile ahead of the scan pass
+    bool have = reduce_pass(0);
     for (int k = 0; have; ++k) {
-      bool have_next = true;
+      const bool have_next = reduce_pass(k + 1);
       const int s = k % STAGES;
-      if constexpr (NR > 0) {
-        // the end of work shows in the tile index of the stage
-        if (!mbar_wait_bounded(&full[s], (k / STAGES) & 1, hdr, tmo, 0ull)) break;
-        if (*s_tile(s) >= ntiles) break;
-      } else {
-        if (more) {
-          more = reduce_pass(nred);
-          if (more) ++nred;
-        }
-        have_next = k + 1 < nred;
-      }
       // scan pass of use k
       if constexpr (Trace::kOn)
         if (w == 0 && lane == 0) trace_now(kTrPWait, *s_tile(s));
       if (!mbar_wait_bounded(&prefb[s], (k / STAGES) & 1, hdr, tmo, 0ull)) break;
-      if constexpr (TK == 1)
-        if (w == 0 && lane == 0) ptx::mbar_arrive(&sgo[s]);
       const long long tile = *s_tile(s);
       if (w == 0 && lane == 0) trace_now(kTrSStart, tile);
       const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(tile, n, head);
@@ -990,70 +934,10 @@ __global__ void __launch_bounds__((NC + NR + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
             *reinterpret_cast<uint4*>(stage + size_t(r0 + c * V) * sizeof(in_t)) = o.u;
           }
         };
-        if constexpr (EXC == 1) {
+        if (excl_kind)
           chain(std::true_type{});
-        } else if constexpr (EXC == 0) {
+        else
           chain(std::false_type{});
-        } else {
-          if (excl_kind)
-            chain(std::true_type{});
-          else
-            chain(std::false_type{});
-        }
-        store_segment(stage, g);
-      } else if constexpr (LAY == 1) {
-        // lane-blocked: this lane's row of CH chunks, one warp scan of the row
-        // totals, results written back in place, then streamed out striped
-        unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
-        const int r0 = w * Cfg::SEG + lane * (CH * V);
-        const bool interior = g.lo == 0 && g.blo == 0 && g.bhi == TILE;
-        acc_t a[CH][V];
-#pragma unroll
-        for (int c = 0; c < CH; ++c) {
-          if (interior) {
-            union {
-              uint4 u;
-              in_t x[V];
-            } buf;
-            buf.u = *reinterpret_cast<const uint4*>(stage + size_t(r0 + c * V) * sizeof(in_t));
-#pragma unroll
-            for (int j = 0; j < V; ++j) a[c][j] = pol.load(buf.x[j]);
-          } else {
-            load_at(s, r0 + c * V, g, a[c]);
-          }
-#pragma unroll
-          for (int j = 1; j < V; ++j) a[c][j] = pol.aop(a[c][j - 1], a[c][j]);
-        }
-        // row prefix before each chunk (kept for small accumulators only)
-        constexpr bool kKeep = sizeof(acc_t) * CH <= 72;
-        acc_t P[kKeep ? CH : 1];
-        acc_t run = a[0][V - 1];
-#pragma unroll
-        for (int c = 1; c < CH; ++c) {
-          if constexpr (kKeep) P[c] = run;
-          run = pol.aop(run, a[c][V - 1]);
-        }
-        const acc_t inc = warp_inclusive_scan(run, aop, lane);
-        acc_t ex = shfl_up(inc, 1);
-        if (lane == 0) ex = pol.aid();
-        const pre_t pl = pol.extend(pw, ex);
-        pre_t cur = pl;
-#pragma unroll
-        for (int c = 0; c < CH; ++c) {
-          pre_t pc;
-          if constexpr (kKeep) {
-            pc = c == 0 ? pl : pol.extend(pl, P[c]);
-          } else {
-            pc = cur;
-            if (c + 1 < CH) cur = pol.extend(cur, a[c][V - 1]);
-          }
-          union {
-            uint4 u;
-            out_t x[V];
-          } o;
-          TileScan<Pol, NC, CH, V>::finish_chunk(pol, pc, a[c], excl_kind, o.x);
-          *reinterpret_cast<uint4*>(stage + size_t(r0 + c * V) * sizeof(in_t)) = o.u;
-        }
         store_segment(stage, g);
       } else {
       acc_t X = pol.aid();

@@ -272,7 +272,7 @@ struct DecoupledTuning {
 };
 template <class Pol>
 using StagedFor = StagedCfg<Pol, DecoupledTuning<Pol>::NC, DecoupledTuning<Pol>::CH, DecoupledTuning<Pol>::STAGES,
-                            DecoupledTuning<Pol>::LBW, DecoupledTuning<Pol>::LAY, 0,
+                            DecoupledTuning<Pol>::LBW, DecoupledTuning<Pol>::LAY,
                             (DecoupledTuning<Pol>::BS == 2 ? 1 : 0)>;
 
 // The staged (bulk-copy) kernel takes any naturally aligned pointers of an
@@ -348,8 +348,7 @@ inline Status decoupled_scan(cudaStream_t s, const void* in, void* out, uint64_t
   if constexpr (16 % sizeof(typename Pol::in_t) == 0) {
     if (tma_path_ok<Pol>(in, out)) {
       using Cfg = StagedFor<Pol>;
-      auto k = decoupled_staged_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Tn::LAY, Tn::TK, 0, Tn::PG, -1,
-                                       Tn::BS>;
+      auto k = decoupled_staged_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Tn::LAY, Tn::TK, Tn::PG, Tn::BS>;
       int bps = 0;
       st = prepare_kernel(k, Cfg::THREADS, Cfg::SMEM, bps);
       if (st != Status::ok) return st;
