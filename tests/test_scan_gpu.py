@@ -225,3 +225,33 @@ def test_bad_arguments(pp, cuda):
     with pytest.raises(pp.PPError) as e:
         pp.scan("inclusive", "plus", d.data_ptr(), d.data_ptr(), 16, "u32", precision="compensated")
     assert e.value.status == pp.PP_ERR_UNSUPPORTED
+
+
+# byte offset of the epoch word in the workspace header (csrc/pp/workspace.cuh:
+# ticket, descriptor high-water mark and error detail are 8 bytes each, the exit
+# counter 4) and the limit after which the epoch wraps to 0
+_EPOCH_OFFSET = 28
+_EPOCH_LIMIT = (1 << 30) - 1
+
+
+def test_epoch_wrap_clears_the_descriptors(pp, oracle, cuda):
+    """A caller-owned workspace whose epoch is three launches from its limit:
+    the launch that crosses it clears every descriptor word used so far and
+    restarts at epoch 0, and the scans on both sides of the wrap stay exact."""
+    sizes = [300000, 1 << 20, 70001, 1 << 20, 5000, 1 << 19]
+    xs = [make_input("u32", "plus", n, seed=40 + i) for i, n in enumerate(sizes)]
+    d_in = [to_dev(cuda, x) for x in xs]
+    d_out = [cuda.empty_like(d) for d in d_in]
+    nbytes = max(pp.workspace_size("decoupled", "u32", a.data_ptr(), b.data_ptr(), a.numel())
+                 for a, b in zip(d_in, d_out))
+    ws = cuda.zeros(nbytes, dtype=cuda.uint8, device="cuda")
+    ws[_EPOCH_OFFSET:_EPOCH_OFFSET + 4] = cuda.tensor(
+        list((_EPOCH_LIMIT - 3).to_bytes(4, "little")), dtype=cuda.uint8, device="cuda")
+    s = cuda.cuda.current_stream().cuda_stream
+    for x, a, b in zip(xs, d_in, d_out):
+        pp.scan("inclusive", "plus", a.data_ptr(), b.data_ptr(), a.numel(), "u32", stream=s, algo="decoupled",
+                workspace=(ws.data_ptr(), nbytes))
+        assert pp.workspace_status(s, ws.data_ptr()) == 0
+        assert np.array_equal(from_dev(b, np.uint32), oracle.scan(x, "plus"))
+    epoch = int.from_bytes(bytes(ws[_EPOCH_OFFSET:_EPOCH_OFFSET + 4].cpu().tolist()), "little")
+    assert epoch == len(sizes) - 3  # limit - 3, - 2, - 1, then 0, 1, 2 after the six launches
