@@ -255,3 +255,46 @@ def test_epoch_wrap_clears_the_descriptors(pp, oracle, cuda):
         assert np.array_equal(from_dev(b, np.uint32), oracle.scan(x, "plus"))
     epoch = int.from_bytes(bytes(ws[_EPOCH_OFFSET:_EPOCH_OFFSET + 4].cpu().tolist()), "little")
     assert epoch == len(sizes) - 3  # limit - 3, - 2, - 1, then 0, 1, 2 after the six launches
+
+
+def _tile_elements(pp, cuda, dtype, precision="default"):
+    """Elements per tile of the kernel the library picks for aligned pointers
+    of this type: the first length whose workspace needs a second descriptor."""
+    d = cuda.empty(16, dtype=cuda.int64, device="cuda")
+    p = d.data_ptr()
+    one = pp.workspace_size("decoupled", dtype, p, p, 1, precision=precision)
+    lo, hi = 1, 1 << 20
+    while lo < hi:  # smallest n with more workspace than n = 1
+        mid = (lo + hi) // 2
+        if pp.workspace_size("decoupled", dtype, p, p, mid, precision=precision) > one:
+            hi = mid
+        else:
+            lo = mid + 1
+    return lo - 1
+
+
+@pytest.mark.parametrize("dtype,precision", [("u32", "default"), ("i32", "default"), ("u64", "default"),
+                                             ("i64", "default"), ("f32", "default"), ("f64", "default"),
+                                             ("f32", "compensated"), ("f32", "fp64_carry")])
+def test_every_policy_at_its_own_tile_edges(pp, oracle, cuda, dtype, precision):
+    """Lengths one below, at and above one, two and three tiles of the
+    configuration each policy runs with (tile sizes differ per policy)."""
+    t = _tile_elements(pp, cuda, dtype, precision)
+    assert t >= 4096
+    s = cuda.cuda.current_stream().cuda_stream
+    for i, n in enumerate([t - 1, t, t + 1, 2 * t - 1, 2 * t + 1, 3 * t + 7]):
+        x = make_input(dtype, "plus", n, seed=70 + i)
+        d_in = to_dev(cuda, x)
+        d_out = cuda.empty_like(d_in)
+        for excl in (False, True):
+            pp.scan("exclusive" if excl else "inclusive", "plus", d_in.data_ptr(), d_out.data_ptr(), n, dtype,
+                    stream=s, algo="decoupled", precision=precision)
+            assert pp.stream_status(s) == 0
+            got = from_dev(d_out, NP[dtype])
+            if precision == "compensated":
+                want = oracle.scan_fp64(x, excl)
+                m = np.abs(want) > 1e-3 * np.sqrt(np.mean(want * want))
+                rel = np.abs(got.astype(np.float64)[m] - want[m]) / np.abs(want[m])
+                assert rel.max() <= 1e-6, (n, excl, rel.max())
+            else:
+                check_scan(got, x, dtype, "plus", excl, _tiles(n))
