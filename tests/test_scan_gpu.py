@@ -298,3 +298,48 @@ def test_every_policy_at_its_own_tile_edges(pp, oracle, cuda, dtype, precision):
                 assert rel.max() <= 1e-6, (n, excl, rel.max())
             else:
                 check_scan(got, x, dtype, "plus", excl, _tiles(n))
+
+
+@pytest.mark.parametrize("dtype,precision", [("u32", "default"), ("u64", "default"), ("f32", "compensated")])
+def test_scan_and_reduce_replayed_from_a_cuda_graph(pp, oracle, cuda, dtype, precision):
+    """A scan and a reduction captured once into a CUDA graph (the stream's
+    workspace sized by ordinary calls first) and replayed with new input
+    contents each time: the descriptor epochs need no reset node between
+    replays."""
+    n = 3 * 16384 * 152 + 12345  # several tiles per CTA
+    stream = cuda.cuda.Stream()
+    x0 = make_input(dtype, "plus", n, seed=90)
+    d_in = to_dev(cuda, x0)
+    d_out = cuda.empty_like(d_in)
+    d_sum = cuda.zeros(2, dtype=cuda.float64 if dtype.startswith("f") else cuda.int64, device="cuda")
+    sh = stream.cuda_stream
+    cuda.cuda.synchronize()
+
+    def body():
+        pp.scan("inclusive", "plus", d_in.data_ptr(), d_out.data_ptr(), n, dtype, stream=sh, algo="decoupled",
+                precision=precision)
+        pp.reduce("plus", d_in.data_ptr(), n, dtype, d_sum.data_ptr(), stream=sh)
+
+    with cuda.cuda.stream(stream):
+        body()
+        stream.synchronize()
+        g = cuda.cuda.CUDAGraph()
+        with cuda.cuda.graph(g, stream=stream):
+            body()
+    for rep in range(3):
+        x = make_input(dtype, "plus", n, seed=91 + rep)
+        d_in.copy_(to_dev(cuda, x))
+        d_out.zero_()
+        cuda.cuda.synchronize()
+        g.replay()
+        cuda.cuda.synchronize()
+        got = from_dev(d_out, NP[dtype])
+        if precision == "compensated":
+            want = oracle.scan_fp64(x)
+            m = np.abs(want) > 1e-3 * np.sqrt(np.mean(want * want))
+            assert (np.abs(got.astype(np.float64)[m] - want[m]) / np.abs(want[m])).max() <= 1e-6
+        else:
+            assert np.array_equal(got, oracle.scan(x, "plus"))
+        if not dtype.startswith("f"):
+            assert from_dev(d_sum, NP[dtype])[0] == oracle.scan(x, "plus")[-1]
+    assert pp.stream_status(sh) == 0
