@@ -71,3 +71,21 @@ def test_views_and_batches(ext, cuda):
     v = x[:, 1:, 1:]  # non-contiguous, offset view
     np.testing.assert_allclose(ext.cumsum(v).cpu().numpy(), cuda.cumsum(v, dim=-1).cpu().numpy(), rtol=1e-5,
                                atol=1e-4)
+
+
+def test_backward_of_long_rows_takes_the_reverse_look_back_kernel(ext, cuda):
+    """Few rows longer than 65,536 elements are not split one warp per row:
+    forward and backward run on the segmented decoupled look-back kernel
+    (the backward in reverse), with tiles crossing row boundaries."""
+    g = cuda.Generator(device="cuda").manual_seed(6)
+    x = cuda.randn(3, 300001, device="cuda", generator=g).requires_grad_(True)
+    up = cuda.randn(3, 300001, device="cuda", generator=g)
+    y = ext.cumsum(x)
+    y.backward(up)
+    ref = cuda.flip(cuda.cumsum(cuda.flip(up.double(), [1]), dim=1), [1])
+    absref = cuda.flip(cuda.cumsum(cuda.flip(up.double().abs(), [1]), dim=1), [1])
+    err = (x.grad.double() - ref).abs()
+    assert bool((err <= (64 + 64) * np.finfo(np.float32).eps * absref + 1e-30).all())
+    fwd = cuda.cumsum(x.detach().double(), dim=1)
+    absfwd = cuda.cumsum(x.detach().double().abs(), dim=1)
+    assert bool(((y.detach().double() - fwd).abs() <= (64 + 64) * np.finfo(np.float32).eps * absfwd + 1e-30).all())
