@@ -482,16 +482,16 @@ inline Status reduce(cudaStream_t s, const T* in, uint64_t n, T* d_result, void*
 // to this kernel (uniform heads, either direction) take 16 warps of 8 16-byte
 // chunks.
 constexpr uint64_t kSegLongMean = 512;
-template <int LAY_, int NC_, int CH_, int VB_, class T, int LBW_ = 4>
+template <int LAY_, int NC_, int CH_, int VB_, class T, int LBW_ = 4, int BS_ = 0>
 struct SegVariant {
-  static constexpr int LAY = LAY_, NC = NC_, CH = CH_, VB = VB_, LBW = LBW_;
+  static constexpr int LAY = LAY_, NC = NC_, CH = CH_, VB = VB_, LBW = LBW_, BS = BS_;
   static constexpr int TILE_BYTES = NC * 32 * CH * VB;
   static constexpr int ST0 = 196608 / TILE_BYTES;
   static constexpr int STAGES = LAY == 2 ? 3 : (ST0 < 2 ? 2 : (ST0 > 8 ? 8 : ST0));
 };
 #define PP_SEG_VARIANT(DT, LEN)                                                                              \
   SegVariant<PP_SEG_##DT##_##LEN##_LAY, PP_SEG_##DT##_##LEN##_NC, PP_SEG_##DT##_##LEN##_CH, PP_SEG_##DT##_##LEN##_VB, \
-             T, PP_SEG_##DT##_##LEN##_LBW>
+             T, PP_SEG_##DT##_##LEN##_LBW, PP_SEG_##DT##_##LEN##_BS>
 template <class T, bool LONG>
 using SegTunedCsr = std::conditional_t<
     std::is_floating_point_v<T>,
@@ -557,8 +557,10 @@ inline Status acquire_scratch(cudaStream_t s, size_t need, unsigned char** out) 
 
 template <class Tn, class Pol, class Heads, bool REVERSE, bool REDUCE>
 inline Status launch_segmented_variant(cudaStream_t s, const SegArgs& a) {
-  using Cfg = SegCfg<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Tn::VB, Tn::LAY>;
-  auto k = segmented_staged_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Heads, REVERSE, REDUCE, Tn::VB, Tn::LAY>;
+  constexpr int BS = REDUCE ? 0 : Tn::BS;  // the store warp serves scans only
+  using Cfg = SegCfg<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Tn::VB, Tn::LAY, (BS == 2 ? 1 : 0)>;
+  auto k =
+      segmented_staged_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Heads, REVERSE, REDUCE, Tn::VB, Tn::LAY, BS>;
   DeviceInfo di;
   Status st = device_info(di);
   if (st != Status::ok) return st;

@@ -86,7 +86,7 @@ struct SegArgs {
 // consecutive 16-byte chunks (CH odd: conflict-free), the reduce pass leaves
 // each row's (value, count) total in shared memory and the scan pass is one
 // thread-serial chain per row (forward scans and reductions with CSR heads).
-template <class Pol, int NC_, int CH_, int STAGES_, int LBW_, int VB_ = 16, int LAY_ = 0>
+template <class Pol, int NC_, int CH_, int STAGES_, int LBW_, int VB_ = 16, int LAY_ = 0, int SW_ = 0>
 struct SegCfg {
   using in_t = typename Pol::in_t;
   using acc_t = typename Pol::acc_t;
@@ -104,7 +104,9 @@ struct SegCfg {
   static_assert(TILE % 128 == 0, "tile must cover whole 16-byte bitmap words");
   static constexpr int TILE_BYTES = TILE * int(sizeof(in_t));
   static constexpr int MAP_BYTES = TILE / 8;  // head bits of one tile
-  static constexpr int THREADS = (NC + 2) * 32;
+  static constexpr int SW = SW_;  // store warps (1: finished tiles leave by one bulk copy, rows scans only)
+  static_assert(SW == 0 || (SW == 1 && LAY_ == 2), "the store warp serves the rows layout");
+  static constexpr int THREADS = (NC + 2 + SW) * 32;
   static constexpr size_t META_AGG = 0;
   static constexpr size_t META_PREF = align_up(NC * sizeof(acc_t), 16);
   static constexpr size_t META_TAGG = META_PREF + align_up(sizeof(carry_t), 16);
@@ -117,15 +119,19 @@ struct SegCfg {
   static constexpr size_t OFF_MAP = size_t(STAGES) * TILE_BYTES;
   static constexpr size_t OFF_META = OFF_MAP + size_t(STAGES) * MAP_BYTES;
   static constexpr size_t OFF_BAR = align_up(OFF_META + STAGES * META_BYTES, 8);
-  static constexpr size_t SMEM = OFF_BAR + 4 * STAGES * 8;
+  static constexpr size_t SMEM = OFF_BAR + 5 * STAGES * 8;  // full, empty, aggb, prefb, scanned
 };
 
 // REDUCE: write only segment totals (via rank_to_seg) instead of the scan.
+// BS: 2 = a store warp writes each finished full tile of a rows-layout scan
+// back with one bulk copy and frees the stage (the compute warps go on to the
+// next tile); 0 = the compute warps store.
 template <class Pol, int NC, int CH, int STAGES, int LBW, class Heads, bool REVERSE, bool REDUCE, int VB = 16,
-          int LAY = 0>
-__global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(const SegArgs sargs) {
-  using Cfg = SegCfg<Pol, NC, CH, STAGES, LBW, VB, LAY>;
+          int LAY = 0, int BS = 0>
+__global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmented_staged_kernel(const SegArgs sargs) {
+  using Cfg = SegCfg<Pol, NC, CH, STAGES, LBW, VB, LAY, (BS == 2 ? 1 : 0)>;
   static_assert(LAY == 0 || (!REVERSE && Heads::kBitmap), "rows: forward scans over CSR heads");
+  static_assert(BS == 0 || (BS == 2 && LAY == 2 && !REDUCE), "the store warp serves rows-layout scans");
   using vec_t = std::conditional_t<VB == 16, uint4, std::conditional_t<VB == 8, uint2, uint32_t>>;
   using in_t = typename Pol::in_t;
   using out_t = typename Pol::out_t;
@@ -144,6 +150,7 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
   uint64_t* empty = bars + STAGES;
   uint64_t* aggb = bars + 2 * STAGES;
   uint64_t* prefb = bars + 3 * STAGES;
+  uint64_t* scanned = bars + 4 * STAGES;  // the compute warps' results are in the stage (BS == 2)
   auto meta = [&](int s) { return smem + Cfg::OFF_META + size_t(s) * Cfg::META_BYTES; };
   auto s_aggs = [&](int s) { return reinterpret_cast<acc_t*>(meta(s) + Cfg::META_AGG); };
   auto s_pref = [&](int s) { return reinterpret_cast<carry_t*>(meta(s) + Cfg::META_PREF); };
@@ -166,9 +173,10 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       ptx::mbar_init(&full[s], 1);
-      ptx::mbar_init(&empty[s], NC);
+      ptx::mbar_init(&empty[s], BS == 2 ? 1 : NC);
       ptx::mbar_init(&aggb[s], NC);
       ptx::mbar_init(&prefb[s], 1);
+      ptx::mbar_init(&scanned[s], NC);
       *s_cnt(s) = 0u;
     }
     ptx::fence_mbar_init();
@@ -240,6 +248,32 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
       if (lane == 0) {
         *s_pref(s) = excl;
         ptx::mbar_arrive(&prefb[s]);
+      }
+      __syncwarp();
+    }
+  } else if (BS == 2 && warp == NC + 2) {
+    // ------------------------------------------------------------ store
+    // Each finished full tile leaves as one bulk copy; the stage is freed as
+    // soon as the copy has read it. A partial tile (or an output that is not
+    // 16-byte aligned) is stored by the compute warps themselves.
+    out_t* gout = static_cast<out_t*>(args.out);
+    const bool out_vec = (reinterpret_cast<uintptr_t>(gout) & 15u) == 0;
+    const uint64_t pol_l2 = ptx::policy_evict_first();
+    for (int k = 0;; ++k) {
+      const int s = k % STAGES;
+      const uint32_t par = (k / STAGES) & 1;
+      if (!mbar_wait_bounded(&full[s], par, hdr, tmo, 0ull)) break;
+      const long long tile = *s_tile(s);
+      if (tile >= ntiles) break;
+      if (!mbar_wait_bounded(&scanned[s], par, hdr, tmo, 0ull)) break;
+      const uint64_t base = uint64_t(phys(tile)) * TILE;
+      if (lane == 0) {
+        if (out_vec && n - base >= uint64_t(TILE)) {
+          ptx::bulk_s2g_hint(gout + base, smem + size_t(s) * Cfg::TILE_BYTES, uint32_t(Cfg::TILE_BYTES), pol_l2);
+          ptx::bulk_commit();
+          ptx::bulk_wait_read<0>();
+        }
+        ptx::mbar_arrive(&empty[s]);
       }
       __syncwarp();
     }
@@ -481,7 +515,11 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
           }
           if constexpr (!REDUCE) *reinterpret_cast<vec_t*>(stage + size_t(e0) * sizeof(in_t)) = o.u;
         }
-        if constexpr (!REDUCE) {
+        if constexpr (BS == 2) {
+          // a full tile with an aligned output leaves by the store warp's bulk copy
+          if ((reinterpret_cast<uintptr_t>(gout) & 15u) == 0 && valid == TILE) ptx::fence_proxy_async_smem();
+        }
+        if (!REDUCE && (BS != 2 || (reinterpret_cast<uintptr_t>(gout) & 15u) != 0 || valid != TILE)) {
           __syncwarp();
 #pragma unroll
           for (int c = 0; c < CH; ++c) {
@@ -586,10 +624,11 @@ __global__ void __launch_bounds__((NC + 2) * 32, 1) segmented_staged_kernel(cons
       }
       }
       __syncwarp();
-      if (lane == 0) ptx::mbar_arrive(&empty[s]);
+      if (lane == 0) ptx::mbar_arrive(BS == 2 ? &scanned[s] : &empty[s]);
       have = have_next;
     }
   }
+  if constexpr (BS == 2) ptx::bulk_wait<0>();  // this thread's bulk stores are complete
   __syncthreads();
   if (threadIdx.x == 0) cta_exit_rearm(hdr, args.desc, uint64_t(ntiles) * codec::W);
 }

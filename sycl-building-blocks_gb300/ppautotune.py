@@ -4,7 +4,8 @@ Compiles tune/seg_autotune.cu once per payload type, in parallel (variants of
 the segmented kernel: striped chunks over compute warps {4, 8, 16} = block size
 {128, 256, 512} threads, items per thread {4, 8, 16, 32} and chunk vector width
 {8, 16} bytes; lane rows over {12, 14, 16, 18, 20} warps with {5, 7, 9} 16-byte
-chunks per lane and look-back polls of {1, 4} windows), runs the binaries one
+chunks per lane, look-back polls of {1, 4} windows and, with one-window polls,
+an optional store warp), runs the binaries one
 after another on the GPU on two length distributions ("long": 65,536
 log-uniform segments in [1, 2^16]; "short": 2^21 segments of U[1, 128]) with
 int32, float32, int64 and float64 payloads, records every measurement in tune/seg_autotune_results.json and
@@ -73,7 +74,7 @@ def choose(rows: list[dict]) -> dict:
                 raise RuntimeError(f"no valid variant for {dt} payloads, {dist} segments")
             b = max(cand, key=lambda r: r["elems_per_s"])
             out[f"{dt}_{dist}"] = {"lay": b["lay"], "nc": b["nc"], "ch": b["ch"], "vb": b["vb"],
-                                   "lbw": b.get("lbw", 4), "elems_per_s": b["elems_per_s"]}
+                                   "lbw": b.get("lbw", 4), "bs": b.get("bs", 0), "elems_per_s": b["elems_per_s"]}
     return out
 
 
@@ -84,7 +85,7 @@ def write_inc(choice: dict, device: str) -> Path:
              "// (see tune/seg_autotune_results.json)."]
     for key, c in choice.items():
         dt, dist = key.split("_")
-        for f in ("lay", "nc", "ch", "vb", "lbw"):
+        for f in ("lay", "nc", "ch", "vb", "lbw", "bs"):
             lines.append(f"#define PP_SEG_{dt.upper()}_{dist.upper()}_{f.upper()} {c[f]}")
     inc.write_text("\n".join(lines) + "\n")
     return inc

@@ -7,7 +7,8 @@
 //     width {8, 16} bytes;
 //   lane rows (LAY 2): compute warps {12, 14, 16, 18, 20}, {5, 7, 9} 16-byte
 //     chunks per lane (items per thread 20 / 28 / 36 for 4-byte payloads),
-//     look-back polls of {1, 4} windows of 32 descriptors.
+//     look-back polls of {1, 4} windows of 32 descriptors, and with one-window
+//     polls also a store warp that writes finished tiles by bulk copy.
 // Distributions: "long" = 65,536 segments with lengths floor(exp(U[0, ln 2^16]))
 // clipped to [1, 2^16] (about 2^28 elements, the batched benchmark), "short" =
 // 2^21 segments with lengths U[1, 128] (about 2^27 elements). Payloads: int32
@@ -56,7 +57,7 @@ __global__ void fill(T* p, uint64_t n, uint64_t seed) {
   }
 }
 
-template <class T, int LAY, int NC, int CH, int VB, int LBW = 4>
+template <class T, int LAY, int NC, int CH, int VB, int LBW = 4, int BS = 0>
 void run_variant(Workload<T>& w, const char* dt, bool is_reference) {
   using Pol = SegPlainScan<T, plus>;
   constexpr int V = VB / int(sizeof(T));
@@ -67,13 +68,13 @@ void run_variant(Workload<T>& w, const char* dt, bool is_reference) {
     constexpr int TILE_BYTES = NC * 32 * ITEMS * int(sizeof(T));
     constexpr int ST0 = 196608 / TILE_BYTES;
     constexpr int STAGES = LAY == 2 ? 3 : (ST0 < 2 ? 2 : (ST0 > 8 ? 8 : ST0));
-    using Cfg = SegCfg<Pol, NC, CH, STAGES, LBW, VB, LAY>;
+    using Cfg = SegCfg<Pol, NC, CH, STAGES, LBW, VB, LAY, (BS == 2 ? 1 : 0)>;
     if constexpr (Cfg::SMEM > 232448 || (Cfg::TILE % 128) != 0) {
       printf("{\"dtype\":\"%s\",\"dist\":\"%s\",\"lay\":%d,\"nc\":%d,\"ch\":%d,\"vb\":%d,\"skipped\":true}\n", dt,
              w.dist, LAY, NC, CH, VB);
       return;
     } else {
-      auto k = segmented_staged_kernel<Pol, NC, CH, STAGES, LBW, CsrHeads, false, false, VB, LAY>;
+      auto k = segmented_staged_kernel<Pol, NC, CH, STAGES, LBW, CsrHeads, false, false, VB, LAY, BS>;
       cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Cfg::SMEM));
       int bps = 0, sms = 0;
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, Cfg::THREADS, Cfg::SMEM);
@@ -125,9 +126,9 @@ void run_variant(Workload<T>& w, const char* dt, bool is_reference) {
       }
       const double med = ms[ms.size() / 2];
       printf("{\"dtype\":\"%s\",\"dist\":\"%s\",\"lay\":%d,\"nc\":%d,\"ch\":%d,\"vb\":%d,\"lbw\":%d,\"items\":%d,"
-             "\"stages\":%d,\"tile\":%d,\"grid\":%u,\"ms\":%.5f,\"elems_per_s\":%.4e,\"gbs\":%.1f,\"err\":%u,"
-             "\"matches_default\":%s}\n",
-             dt, w.dist, LAY, NC, CH, VB, LBW, ITEMS, STAGES, Cfg::TILE, grid, med, double(w.n) / (med * 1e-3),
+             "\"bs\":%d,\"stages\":%d,\"tile\":%d,\"grid\":%u,\"ms\":%.5f,\"elems_per_s\":%.4e,\"gbs\":%.1f,"
+             "\"err\":%u,\"matches_default\":%s}\n",
+             dt, w.dist, LAY, NC, CH, VB, LBW, ITEMS, BS, STAGES, Cfg::TILE, grid, med, double(w.n) / (med * 1e-3),
              2.0 * w.n * sizeof(T) / (med * 1e-3) / 1e9, err, same ? "true" : "false");
       fflush(stdout);
       cudaEventDestroy(e0);
@@ -158,6 +159,9 @@ void run_rows(Workload<T>& w, const char* dt) {
   run_variant<T, 2, NC, 5, 16, 1>(w, dt, false);
   run_variant<T, 2, NC, 7, 16, 1>(w, dt, false);
   run_variant<T, 2, NC, 9, 16, 1>(w, dt, false);
+  run_variant<T, 2, NC, 5, 16, 1, 2>(w, dt, false);
+  run_variant<T, 2, NC, 7, 16, 1, 2>(w, dt, false);
+  run_variant<T, 2, NC, 9, 16, 1, 2>(w, dt, false);
 }
 
 template <class T>
