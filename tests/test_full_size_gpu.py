@@ -71,3 +71,29 @@ def test_f32_compensated_2p28_error(pp, oracle, cuda):
     m = np.abs(want) >= 1e-3 * np.sqrt(np.mean(want * want))
     rel = np.abs(got[m] - want[m]) / np.abs(want[m])
     assert rel.max() <= 1e-6, rel.max()
+
+
+def test_u32_scan_and_sum_beyond_2p32_elements(pp, cuda):
+    """2^32 + 12,345 elements (16 GiB in, 16 GiB out): element and tile
+    indices past 32 bits. Checked on the device through properties: wrapping
+    differences of neighbouring outputs give back the input, the first output
+    is the first input, the last is the total, and the reduction agrees."""
+    n = (1 << 32) + 12345
+    g = cuda.Generator(device="cuda")
+    g.manual_seed(33)
+    d_in = cuda.randint(-(1 << 31), (1 << 31) - 1, (n,), dtype=cuda.int32, device="cuda", generator=g)
+    d_out = cuda.empty_like(d_in)
+    s = cuda.cuda.current_stream().cuda_stream
+    pp.decoupled_scan_device("inclusive", "plus", d_in.data_ptr(), d_out.data_ptr(), n, "u32", stream=s)
+    assert pp.stream_status(s) == 0
+    assert int(d_out[0]) == int(d_in[0])
+    step = 1 << 28  # compare in slices to bound the temporaries
+    for a in range(1, n, step):
+        b = min(n, a + step)
+        assert cuda.equal(d_out[a:b] - d_out[a - 1:b - 1], d_in[a:b]), a  # int32 arithmetic wraps like uint32
+    total = int(d_in.sum(dtype=cuda.int64)) & 0xFFFFFFFF
+    assert int(d_out[-1]) & 0xFFFFFFFF == total
+    r = cuda.zeros(1, dtype=cuda.int64, device="cuda")
+    pp.reduce("plus", d_in.data_ptr(), n, "u32", r.data_ptr(), stream=s)
+    assert pp.stream_status(s) == 0
+    assert int(r[0]) & 0xFFFFFFFF == total
