@@ -97,3 +97,21 @@ def test_u32_scan_and_sum_beyond_2p32_elements(pp, cuda):
     pp.reduce("plus", d_in.data_ptr(), n, "u32", r.data_ptr(), stream=s)
     assert pp.stream_status(s) == 0
     assert int(r[0]) & 0xFFFFFFFF == total
+
+
+def test_u64_scan_beyond_2p32_elements(pp, cuda):
+    """2^32 + 7 uint64 elements (32 GiB in, 32 GiB out) on the rows layout
+    with the store warp: wrapping differences give back the input."""
+    n = (1 << 32) + 7
+    g = cuda.Generator(device="cuda")
+    g.manual_seed(34)
+    d_in = cuda.randint(-(1 << 62), 1 << 62, (n,), dtype=cuda.int64, device="cuda", generator=g)
+    d_out = cuda.empty_like(d_in)
+    s = cuda.cuda.current_stream().cuda_stream
+    pp.decoupled_scan_device("inclusive", "plus", d_in.data_ptr(), d_out.data_ptr(), n, "u64", stream=s)
+    assert pp.stream_status(s) == 0
+    assert int(d_out[0]) == int(d_in[0])
+    step = 1 << 27
+    for a in range(1, n, step):
+        b = min(n, a + step)
+        assert cuda.equal(d_out[a:b] - d_out[a - 1:b - 1], d_in[a:b]), a  # int64 arithmetic wraps like uint64
