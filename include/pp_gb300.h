@@ -183,8 +183,7 @@ const char* pp_version(void);
  * of a cudaMalloc'd or per-stream cached workspace, so it allocates nothing.
  * Limit: n up to 1,870,659,581 elements of a 4-byte integer type,
  * 2,104,492,029 floats, 511,508,479 elements of an 8-byte integer type or
- * 460,357,631 doubles; larger n
- * returns PP_ERR_WORKSPACE. All calls share the
+ * 460,357,631 doubles; larger n returns PP_ERR_WORKSPACE. All calls share the
  * array: calls that overlap on the GPU race, so order them on one stream.
  * The first call on each device looks up the array's address; make it
  * outside stream capture. Device-side timeouts of this variant are not
