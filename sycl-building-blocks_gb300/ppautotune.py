@@ -107,8 +107,10 @@ def main() -> None:
         except Exception:
             device = "unknown GPU"
     choice = choose(rows)
-    results.write_text(json.dumps({"device": device, "seconds": seconds, "choice": choice, "rows": rows},
-                                  indent=1) + "\n")
+    # one measurement per line
+    body = ",\n  ".join(json.dumps(r, separators=(",", ":")) for r in rows)
+    head = json.dumps({"device": device, "seconds": seconds, "choice": choice}, indent=1)[:-2]
+    results.write_text(head + ',\n "rows": [\n  ' + body + "\n ]\n}\n")
     print(write_inc(choice, device), choice)
 
 
