@@ -597,7 +597,7 @@ def bench_cumsum(torch, stream, steps) -> dict:
         cur.wait_stream(side)
         gr = torch.cuda.CUDAGraph()
         x.grad = None
-        with torch.cuda.graph(gr):
+        with torch.cuda.graph(gr, stream=side):  # the stream the warm-up sized the library's workspace on
             fn()
         return gr
 

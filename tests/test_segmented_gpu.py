@@ -113,6 +113,31 @@ def test_rows_scan(pp, oracle, cuda, dtype, shape, reverse):
             _check_segment(np.ascontiguousarray(g), np.ascontiguousarray(row), dtype, "plus", excl, oracle)
 
 
+@pytest.mark.parametrize("dtype,cols", [("f32", 1024), ("i32", 2048), ("f32", 4096), ("u32", 8192), ("f32", 16384),
+                                        ("f64", 512), ("i64", 2048), ("u64", 8192)])
+@pytest.mark.parametrize("rows", [1, 17, 37])
+@pytest.mark.parametrize("reverse", [False, True])
+def test_rows_that_tile_a_stage(pp, oracle, cuda, dtype, cols, rows, reverse):
+    """Row lengths that are 1, 2, 4, 8 or 16 compute-warp segments take the
+    tile-of-rows kernel: whole rows per 64 KB tile, the segments of a row
+    exchanging totals; row counts that leave the last tile partly empty."""
+    op = "maximum" if dtype == "i32" else "plus"
+    x = make_input(dtype, op, rows * cols, seed=rows * 31 + cols)
+    d_in = to_dev(cuda, x)
+    d_out = cuda.empty_like(d_in)
+    s = cuda.cuda.current_stream().cuda_stream
+    for excl in (False, True):
+        pp.rows_scan("exclusive" if excl else "inclusive", op, d_in.data_ptr(), d_out.data_ptr(), rows, cols, dtype,
+                     reverse=reverse, stream=s)
+        assert pp.stream_status(s) == 0
+        got = from_dev(d_out, NP[dtype]).reshape(rows, cols)
+        xm = x.reshape(rows, cols)
+        for r in range(rows):
+            row = xm[r, ::-1] if reverse else xm[r]
+            g = got[r, ::-1] if reverse else got[r]
+            _check_segment(np.ascontiguousarray(g), np.ascontiguousarray(row), dtype, op, excl, oracle)
+
+
 def test_rows_scan_max(pp, oracle, cuda):
     rows, cols = 9, 30000
     x = make_input("i32", "maximum", rows * cols, seed=5)
@@ -154,3 +179,33 @@ def test_segmented_scan_in_cuda_graph(pp, oracle, cuda):
             a, b = off[k], off[k + 1]
             np.testing.assert_array_equal(got[a:b], oracle.scan(x[a:b], "plus"))
     assert pp.stream_status(stream.cuda_stream) == 0
+
+
+@pytest.mark.parametrize("warmed_stream", [True, False])
+def test_rows_scan_in_cuda_graph(pp, oracle, cuda, warmed_stream):
+    """Row scans captured into a CUDA graph: on the stream the warm-up sized
+    the workspace on (the whole-row tile kernel), or on a fresh capture
+    stream (the kernels that need no workspace)."""
+    rows, cols = 96, 8192
+    x = make_input("f32", "plus", rows * cols, seed=8)
+    d_in = to_dev(cuda, x)
+    d_out = cuda.empty_like(d_in)
+    side = cuda.cuda.Stream()
+    side.wait_stream(cuda.cuda.current_stream())
+    with cuda.cuda.stream(side):
+        pp.rows_scan("inclusive", "plus", d_in.data_ptr(), d_out.data_ptr(), rows, cols, "f32",
+                     stream=side.cuda_stream)
+    cuda.cuda.current_stream().wait_stream(side)
+    cuda.cuda.synchronize()
+    g = cuda.cuda.CUDAGraph()
+    cap = side if warmed_stream else cuda.cuda.Stream()
+    with cuda.cuda.graph(g, stream=cap):
+        pp.rows_scan("inclusive", "plus", d_in.data_ptr(), d_out.data_ptr(), rows, cols, "f32",
+                     stream=cap.cuda_stream)
+    d_out.zero_()
+    cuda.cuda.synchronize()
+    g.replay()
+    cuda.cuda.synchronize()
+    got = from_dev(d_out, np.float32).reshape(rows, cols)
+    for r in range(0, rows, 7):
+        _check_segment(got[r], np.ascontiguousarray(x.reshape(rows, cols)[r]), "f32", "plus", False, oracle)
