@@ -1,13 +1,15 @@
-// Independent scans of the rows of a row-major matrix, one warp per row.
+// Independent scans of the rows of a row-major matrix.
 //
-// A row of a few hundred or more elements is long enough to keep a warp
-// streaming, and a matrix with many rows has enough of them to fill the GPU,
-// so no row needs to wait for another: each warp walks its row front to back
-// (or back to front for reverse scans) in steps of 32 lanes x V elements,
-// carrying the running prefix in a register. Loads for U steps are issued
-// before the first of them is scanned, which keeps U x 512 bytes per warp in
-// flight; with 48 warps per SM that is enough to stream at HBM speed. Short
-// rows or few long rows take the segmented decoupled-look-back kernel
+// rows_warp_kernel: one warp per row. A row of a few hundred or more elements
+// is long enough to keep a warp streaming, and a matrix with many rows has
+// enough of them to fill the GPU, so no row needs to wait for another: each
+// warp walks its row front to back (or back to front for reverse scans) in
+// steps of 32 lanes x V elements, carrying the running prefix in a register.
+// Loads for U steps are issued before the first of them is scanned, which
+// keeps U x 512 bytes per warp in flight.
+// rows_tile_kernel (below): rows whose length tiles a 64 KB shared-memory
+// stage stream through a ring of stages as contiguous whole-row tiles.
+// Short rows or few long rows take the segmented decoupled-look-back kernel
 // instead (the host picks).
 #pragma once
 
