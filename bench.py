@@ -758,7 +758,7 @@ def run_profile_cases(args) -> dict:
                                                                                    o.data_ptr(), n, "u32", stream=sh))
     case("f32 sum reduce 2^26", lambda: pp.reduce("plus", f.data_ptr(), n, "f32", res.data_ptr(), stream=sh))
     case("u64 sum reduce 2^25", lambda: pp.reduce("plus", w.data_ptr(), n // 2, "u64", res.data_ptr(), stream=sh))
-    segs = 16384
+    segs = 65536  # log-uniform lengths in [1, 2^13]: about 60 M elements (240 MB), twice the L2
     gc = torch.Generator(device="cpu").manual_seed(0x5EC)
     lens = torch.floor(torch.exp(torch.rand(segs, generator=gc, dtype=torch.float64) * math.log(2 ** 13)))
     offs = torch.zeros(segs + 1, dtype=torch.int64)

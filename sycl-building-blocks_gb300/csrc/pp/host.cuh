@@ -513,7 +513,7 @@ using SegCfgOf = SegCfg<SegPlainScan<T, Op>, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW
 // nonempty flags, ranks, rank -> segment map.
 struct SegWsLayout {
   size_t control_bytes;
-  size_t bitmap_off, bitmap_bytes, nonempty_off, rank_off, r2s_off, scratch_bytes;
+  size_t bitmap_off, bitmap_bytes, nonempty_off, rank_off, rank_out_off, scratch_bytes;
 };
 template <class T, class Op>
 inline SegWsLayout seg_ws_layout(uint64_t n, uint64_t num_segments, bool csr, bool reduce) {
@@ -542,8 +542,8 @@ inline SegWsLayout seg_ws_layout(uint64_t n, uint64_t num_segments, bool csr, bo
   if (reduce) off += align_up(num_segments * 4, 256);
   L.rank_off = off;
   if (reduce) off += align_up(num_segments * 4, 256);
-  L.r2s_off = off;
-  if (reduce) off += align_up(num_segments * 4, 256);
+  L.rank_out_off = off;  // reduce: totals by rank
+  if (reduce) off += align_up(num_segments * sizeof(T), 256);
   L.scratch_bytes = off;
   return L;
 }
@@ -642,7 +642,7 @@ inline Status segmented_reduce(cudaStream_t s, const T* in, uint64_t n, const in
   uint32_t* heads = reinterpret_cast<uint32_t*>(base + L.bitmap_off);
   uint32_t* nonempty = reinterpret_cast<uint32_t*>(base + L.nonempty_off);
   uint32_t* rank = reinterpret_cast<uint32_t*>(base + L.rank_off);
-  uint32_t* r2s = reinterpret_cast<uint32_t*>(base + L.r2s_off);
+  T* by_rank = reinterpret_cast<T*>(base + L.rank_out_off);
   if (cudaMemsetAsync(heads, 0, L.bitmap_bytes, s) != cudaSuccess) return Status::cuda;
   const unsigned pre_grid = unsigned((num_segments + 255) / 256 < 1024 ? (num_segments + 255) / 256 : 1024);
   segment_heads_kernel<T, Op><<<pre_grid, 256, 0, s>>>(offsets, num_segments, n, heads, nonempty, out);
@@ -650,8 +650,6 @@ inline Status segmented_reduce(cudaStream_t s, const T* in, uint64_t n, const in
   if (n == 0) return Status::ok;
   st = decoupled_scan<PlainScan<uint32_t, plus>>(s, nonempty, rank, num_segments, true, w.hdr, L.control_bytes);
   if (st != Status::ok) return st;
-  segment_rank_kernel<<<pre_grid, 256, 0, s>>>(nonempty, rank, num_segments, r2s);
-  if (cudaGetLastError() != cudaSuccess) return Status::cuda;
   SegArgs a{};
   a.s.in = in;
   a.s.out = nullptr;
@@ -661,9 +659,11 @@ inline Status segmented_reduce(cudaStream_t s, const T* in, uint64_t n, const in
   a.s.timeout_ns = settings().timeout_ns.load();
   a.s.debug_skip_tile = -1;
   a.heads = heads;
-  a.rank_to_seg = r2s;
-  a.seg_out = out;
-  return launch_segmented<SegPlainScan<T, Op>, CsrHeads, false, true>(s, a, num_segments);
+  a.rank_out = by_rank;
+  st = launch_segmented<SegPlainScan<T, Op>, CsrHeads, false, true>(s, a, num_segments);
+  if (st != Status::ok) return st;
+  segment_gather_kernel<T><<<pre_grid, 256, 0, s>>>(nonempty, rank, by_rank, num_segments, out);
+  return from_cuda(cudaGetLastError());
 }
 
 // Row scans of a rows x cols row-major matrix (every row its own segment);

@@ -24,8 +24,9 @@
 //
 // Segmented reduce reuses the same pass without writing the scanned array:
 // the element that ends a non-empty segment writes the segment's value to
-// out[rank_to_segment[count - 1]]; empty segments get the identity from the
-// pre-pass.
+// rank_out[count - 1] (its rank among the non-empty segments: a store with no
+// load in front of it), and segment_gather_kernel moves the totals to their
+// segments; empty segments get the identity from the pre-pass.
 #pragma once
 
 #include <cstdint>
@@ -76,8 +77,7 @@ struct SegArgs {
   ScanArgs s;
   const uint32_t* heads;         // CSR: n-bit head bitmap (tile-padded), else null
   uint64_t seg_len;              // uniform: row length
-  const uint32_t* rank_to_seg;   // reduce: non-empty segment rank -> segment id
-  void* seg_out;                 // reduce: per-segment output
+  void* rank_out;                // reduce: total of each non-empty segment, by rank
 };
 
 // NC compute warps, CH chunks per lane, VB bytes per chunk (the vector width
@@ -122,7 +122,7 @@ struct SegCfg {
   static constexpr size_t SMEM = OFF_BAR + 5 * STAGES * 8;  // full, empty, aggb, prefb, scanned
 };
 
-// REDUCE: write only segment totals (via rank_to_seg) instead of the scan.
+// REDUCE: write only segment totals (by rank) instead of the scan.
 // BS: 2 = a store warp writes each finished full tile of a rows-layout scan
 // back with one bulk copy and frees the stage (the compute warps go on to the
 // next tile); 0 = the compute warps store.
@@ -474,6 +474,8 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
         uint32_t hb_next = 0;
         in_t xn[V];
         if constexpr (REDUCE) hb_next = load_row_chunk(s, r0, base, valid, bulk, xn);
+        // a full tile that is not the array's last: no element is past the end
+        const bool interior = valid == TILE && base + uint64_t(TILE) < n;
 #pragma unroll
         for (int c = 0; c < CH; ++c) {
           in_t x[V];
@@ -491,6 +493,22 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
             vec_t u;
             out_t v[V];
           } o;
+          // reduce: bit j set when element e0 + j ends its segment (the next
+          // element is a head, or it is the array's last element)
+          uint32_t ends = 0;
+          if constexpr (REDUCE) {
+            ends = (hb >> 1) | ((c + 1 < CH ? (hb_next & 1u) : uint32_t(next_head_after_row)) << (V - 1));
+            if (!interior) {
+#pragma unroll
+              for (int j = 0; j < V; ++j) {
+                const int e = e0 + j;
+                if (e >= valid)
+                  ends &= ~(1u << j);
+                else if (base + uint64_t(e) + 1 >= n)
+                  ends |= 1u << j;
+              }
+            }
+          }
 #pragma unroll
           for (int j = 0; j < V; ++j) {
             const bool head = (hb >> j) & 1u;
@@ -499,18 +517,7 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
             if constexpr (!REDUCE) {
               o.v[j] = excl_kind ? (head ? pol.aid().v : before.v) : p.v;
             } else {
-              const int e = e0 + j;
-              if (e < valid) {
-                bool end;
-                if (base + uint64_t(e) + 1 >= n) end = true;
-                else if (j + 1 < V) end = (hb >> (j + 1)) & 1u;
-                else if (c + 1 < CH) end = hb_next & 1u;
-                else end = next_head_after_row;
-                if (end && p.c > 0) {
-                  const uint32_t seg = __ldg(sargs.rank_to_seg + (p.c - 1));
-                  static_cast<out_t*>(sargs.seg_out)[seg] = p.v;
-                }
-              }
+              if (((ends >> j) & 1u) && p.c > 0) static_cast<out_t*>(sargs.rank_out)[p.c - 1] = p.v;
             }
           }
           if constexpr (!REDUCE) *reinterpret_cast<vec_t*>(stage + size_t(e0) * sizeof(in_t)) = o.u;
@@ -614,10 +621,7 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
             }
             if (end) {
               const acc_t v = pol.aop(pc, a[j]);
-              if (v.c > 0) {
-                const uint32_t seg = __ldg(sargs.rank_to_seg + (v.c - 1));
-                static_cast<out_t*>(sargs.seg_out)[seg] = v.v;
-              }
+              if (v.c > 0) static_cast<out_t*>(sargs.rank_out)[v.c - 1] = v.v;
             }
           }
         }
@@ -654,13 +658,14 @@ __global__ void segment_heads_kernel(const int64_t* offsets, uint64_t num_segmen
   }
 }
 
-// rank_to_seg[rank[s]] = s for every non-empty segment (rank = exclusive scan
-// of nonempty).
-template <class I>
-__global__ void segment_rank_kernel(const I* nonempty, const I* rank, uint64_t num_segments, I* rank_to_seg) {
+// out[s] = rank_out[rank[s]] for every non-empty segment (rank = exclusive
+// scan of nonempty).
+template <class T>
+__global__ void segment_gather_kernel(const uint32_t* nonempty, const uint32_t* rank, const T* rank_out,
+                                      uint64_t num_segments, T* out) {
   for (uint64_t s = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; s < num_segments;
        s += uint64_t(gridDim.x) * blockDim.x)
-    if (nonempty[s]) rank_to_seg[rank[s]] = I(s);
+    if (nonempty[s]) out[s] = rank_out[rank[s]];
 }
 
 }  // namespace pp
