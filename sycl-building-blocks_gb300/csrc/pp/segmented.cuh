@@ -126,8 +126,11 @@ struct SegCfg {
 // BS: 2 = a store warp writes each finished full tile of a rows-layout scan
 // back with one bulk copy and frees the stage (the compute warps go on to the
 // next tile); 0 = the compute warps store.
+// SKIP (rows layout): a warp whose chunks hold no segment head (and, in the
+// second pass of a reduction, no segment end) combines them without the
+// per-element head tests; it pays off when segments are long.
 template <class Pol, int NC, int CH, int STAGES, int LBW, class Heads, bool REVERSE, bool REDUCE, int VB = 16,
-          int LAY = 0, int BS = 0>
+          int LAY = 0, int BS = 0, bool SKIP = false>
 __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmented_staged_kernel(const SegArgs sargs) {
   using Cfg = SegCfg<Pol, NC, CH, STAGES, LBW, VB, LAY, (BS == 2 ? 1 : 0)>;
   static_assert(LAY == 0 || (!REVERSE && Heads::kBitmap), "rows: forward scans over CSR heads");
@@ -401,8 +404,15 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
         for (int c = 0; c < CH; ++c) {
           in_t x[V];
           const uint32_t hb = load_row_chunk(s, r0 + c * V, base, valid, bulk, x);
+          if (!SKIP || __any_sync(kFullMask, hb != 0u)) {
 #pragma unroll
-          for (int j = 0; j < V; ++j) r = pol.aop(r, pol.load(x[j], (hb >> j) & 1u));
+            for (int j = 0; j < V; ++j) r = pol.aop(r, pol.load(x[j], (hb >> j) & 1u));
+          } else {
+            // no head in any of the warp's chunks: the same combines with the
+            // head bits known to be zero
+#pragma unroll
+            for (int j = 0; j < V; ++j) r = pol.aop(r, pol.load(x[j], false));
+          }
         }
         const acc_t inc = warp_inclusive_scan(r, aop, lane);
         const acc_t ex = shfl_up(inc, 1);
@@ -509,15 +519,30 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
               }
             }
           }
+          if (!SKIP || __any_sync(kFullMask, (hb | ends) != 0u)) {
 #pragma unroll
-          for (int j = 0; j < V; ++j) {
-            const bool head = (hb >> j) & 1u;
-            const acc_t before = p;
-            p = pol.aop(p, pol.load(x[j], head));
-            if constexpr (!REDUCE) {
-              o.v[j] = excl_kind ? (head ? pol.aid().v : before.v) : p.v;
-            } else {
-              if (((ends >> j) & 1u) && p.c > 0) static_cast<out_t*>(sargs.rank_out)[p.c - 1] = p.v;
+            for (int j = 0; j < V; ++j) {
+              const bool head = (hb >> j) & 1u;
+              const acc_t before = p;
+              p = pol.aop(p, pol.load(x[j], head));
+              if constexpr (!REDUCE) {
+                o.v[j] = excl_kind ? (head ? pol.aid().v : before.v) : p.v;
+              } else {
+                if (((ends >> j) & 1u) && p.c > 0) static_cast<out_t*>(sargs.rank_out)[p.c - 1] = p.v;
+              }
+            }
+          } else {
+            // no head and no segment end in any of the warp's chunks: the
+            // same chain with those bits known to be zero
+#pragma unroll
+            for (int j = 0; j < V; ++j) {
+              if constexpr (REDUCE) {
+                p = pol.aop(p, pol.load(x[j], false));
+              } else {
+                const acc_t before = p;
+                p = pol.aop(p, pol.load(x[j], false));
+                o.v[j] = excl_kind ? before.v : p.v;
+              }
             }
           }
           if constexpr (!REDUCE) *reinterpret_cast<vec_t*>(stage + size_t(e0) * sizeof(in_t)) = o.u;

@@ -63,9 +63,13 @@ def test_segmented_scan(pp, oracle, cuda, dtype, op):
 
 @pytest.mark.parametrize("dtype", DTYPES)
 @pytest.mark.parametrize("op", OPS)
-def test_segmented_reduce(pp, oracle, cuda, dtype, op):
-    rng = np.random.default_rng(7 + len(op))
-    lens = _lengths(rng, 1500, 5000, p_empty=0.15)
+# mean lengths about 30, 530 and 3,000 elements: the short-segment variant,
+# the boundary of the two classes (512), and the long-segment variant whose
+# warps skip the head tests on chunks without segment heads or ends
+@pytest.mark.parametrize("count,max_len", [(3000, 60), (1500, 5000), (300, 30000)])
+def test_segmented_reduce(pp, oracle, cuda, dtype, op, count, max_len):
+    rng = np.random.default_rng(7 + len(op) + max_len)
+    lens = _lengths(rng, count, max_len, p_empty=0.15)
     lens[0] = 0
     lens[-1] = 0
     lens[10] = 50000
