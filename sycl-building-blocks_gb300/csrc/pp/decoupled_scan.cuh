@@ -798,6 +798,9 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
             if (e0 + j >= g.lo && e0 + j < g.valid) gout[g.gbase + e0 + j] = o.x[j];
         }
       }
+      // the stage was written through the generic proxy; the next bulk copy
+      // into it is an async-proxy write
+      ptx::fence_proxy_async_smem();
     };
     // aggregate of segment seg of stage s (a warp-wide value)
     auto reduce_segment = [&](int s, int seg, const StagedGeom& g) -> acc_t {

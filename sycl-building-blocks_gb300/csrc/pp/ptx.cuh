@@ -150,7 +150,8 @@ template <int N>
 __device__ __forceinline__ void bulk_wait() {
   asm volatile("cp.async.bulk.wait_group %0;" ::"n"(N) : "memory");
 }
-// Orders generic-proxy shared-memory writes before later async-proxy reads.
+// Orders this thread's generic-proxy shared-memory accesses before later
+// async-proxy (bulk copy) accesses to the same memory.
 __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }

@@ -145,6 +145,7 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
   constexpr int TILE = Cfg::TILE;
   static_assert(!(REVERSE && Heads::kBitmap), "reverse scans are provided for uniform segments");
   static_assert(!(REVERSE && REDUCE), "reverse segmented reduce is not provided");
+  static_assert(!(REDUCE && LAY == 2) || CH * V <= 32, "a lane row's head and end bits fit one word");
 
   const ScanArgs& args = sargs.s;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -386,6 +387,36 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
       if (e0 + V > valid) hb &= (e0 >= valid) ? 0u : ((1u << (valid - e0)) - 1u);
       return hb;
     };
+    // reduce: bit j set when element e0 + j ends its segment (the next
+    // element is a head, or e0 + j is the array's last element)
+    auto end_bits = [&](int s, int e0, uint64_t base, int valid) -> uint32_t {
+      if (e0 + V < valid) {
+        // e0 is a multiple of V and V divides 32: bits e0 .. e0+V-1 share a word
+        const uint32_t here = s_map(s)[e0 >> 5] >> (e0 & 31);
+        const uint32_t next = (s_map(s)[(e0 + V) >> 5] >> ((e0 + V) & 31)) & 1u;
+        return ((here >> 1) & ((1u << (V - 1)) - 1u)) | (next << (V - 1));
+      }
+      uint32_t en = 0;
+#pragma unroll
+      for (int j = 0; j < V; ++j) {
+        const int e = e0 + j;
+        if (e < valid) {
+          const uint64_t g = base + uint64_t(e) + 1;
+          uint32_t b;
+          if (g >= n)
+            b = 1u;
+          else if (e + 1 < valid)
+            b = (s_map(s)[(e + 1) >> 5] >> ((e + 1) & 31)) & 1u;
+          else
+            b = (__ldg(sargs.heads + (g >> 5)) >> (g & 31)) & 1u;  // first element of the next tile
+          en |= b << j;
+        }
+      }
+      return en;
+    };
+    // reduce: head and end bits of this lane's row in the tile of the last
+    // reduce pass (bit c * V + j for element j of chunk c)
+    uint32_t row_heads = 0, row_ends = 0;
     auto reduce_pass = [&](int k) -> bool {
       const int s = k % STAGES;
       if (!mbar_wait_bounded(&full[s], (k / STAGES) & 1, hdr, tmo, 0ull)) return false;
@@ -400,18 +431,48 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
         // over the segment is done here, and each row's exclusive prefix stays
         // for the scan pass
         const int r0 = w * Cfg::SEG + lane * (CH * V);
+        if constexpr (REDUCE) {
+          // the only pass over the data: a chunk holding segment ends leaves
+          // the row's running value in place of its elements (the stage is
+          // not read again but for those), and the row's head and end bits
+          // are kept for the totals
+          unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
+          uint32_t hpk = 0, epk = 0;
 #pragma unroll
-        for (int c = 0; c < CH; ++c) {
-          in_t x[V];
-          const uint32_t hb = load_row_chunk(s, r0 + c * V, base, valid, bulk, x);
-          if (!SKIP || __any_sync(kFullMask, hb != 0u)) {
+          for (int c = 0; c < CH; ++c) {
+            const int e0 = r0 + c * V;
+            in_t x[V];
+            const uint32_t hb = load_row_chunk(s, e0, base, valid, bulk, x);
+            const uint32_t en = end_bits(s, e0, base, valid);
+            hpk |= hb << (c * V);
+            epk |= en << (c * V);
+            if (!SKIP || __any_sync(kFullMask, (hb | en) != 0u)) {
+              union {
+                vec_t u;
+                out_t v[V];
+              } o;
+#pragma unroll
+              for (int j = 0; j < V; ++j) {
+                r = pol.aop(r, pol.load(x[j], (hb >> j) & 1u));
+                o.v[j] = r.v;
+              }
+              if (en) *reinterpret_cast<vec_t*>(stage + size_t(e0) * sizeof(in_t)) = o.u;
+            } else {
+              // no head and no end in any of the warp's chunks: the same
+              // combines with those bits known to be zero
+#pragma unroll
+              for (int j = 0; j < V; ++j) r = pol.aop(r, pol.load(x[j], false));
+            }
+          }
+          row_heads = hpk;
+          row_ends = epk;
+        } else {
+#pragma unroll
+          for (int c = 0; c < CH; ++c) {
+            in_t x[V];
+            const uint32_t hb = load_row_chunk(s, r0 + c * V, base, valid, bulk, x);
 #pragma unroll
             for (int j = 0; j < V; ++j) r = pol.aop(r, pol.load(x[j], (hb >> j) & 1u));
-          } else {
-            // no head in any of the warp's chunks: the same combines with the
-            // head bits known to be zero
-#pragma unroll
-            for (int j = 0; j < V; ++j) r = pol.aop(r, pol.load(x[j], false));
           }
         }
         const acc_t inc = warp_inclusive_scan(r, aop, lane);
@@ -456,6 +517,7 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
 
     bool have = reduce_pass(0);
     for (int k = 0; have; ++k) {
+      const uint32_t cur_heads = row_heads, cur_ends = row_ends;  // tile k
       const bool have_next = reduce_pass(k + 1);
       const int s = k % STAGES;
       if (!mbar_wait_bounded(&prefb[s], (k / STAGES) & 1, hdr, tmo, 0ull)) break;
@@ -465,109 +527,70 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
       tile_geom(s, tile, base, valid, bulk, mt);
       const acc_t pw = w == 0 ? *s_pref(s) : pol.aop(*s_pref(s), s_aggs(s)[w]);
       if constexpr (LAY == 2) {
-        // the row's prefix inside the segment comes from the reduce pass; a
-        // thread-serial chain per row
         unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
         const int r0 = w * Cfg::SEG + lane * (CH * V);
+        // the row's prefix inside the segment comes from the reduce pass
         acc_t p = pol.aop(pw, s_rows(s)[w * 32 + lane]);
-        // head bit of the element after this row (next lane's first, or the
-        // next tile's first from the global bitmap)
-        bool next_head_after_row = false;
         if constexpr (REDUCE) {
-          const int e1 = r0 + CH * V;
-          if (e1 < valid) {
-            next_head_after_row = (s_map(s)[e1 >> 5] >> (e1 & 31)) & 1u;
-          } else if (base + uint64_t(e1) < n) {
-            next_head_after_row = (__ldg(sargs.heads + ((base + uint64_t(e1)) >> 5)) >> ((base + e1) & 31)) & 1u;
+          // totals of the segments that end in this row, from the running
+          // values the reduce pass left at their last elements; the segment
+          // that is open where the row begins (no head in the row up to its
+          // end) adds the row's prefix
+          for (uint32_t m = cur_ends; m != 0u; m &= m - 1u) {
+            const int i = __ffs(m) - 1;
+            const uint32_t h = __popc(cur_heads & (0xFFFFFFFFu >> (31 - i)));  // heads up to element i
+            acc_t t = pol.load(reinterpret_cast<const out_t*>(stage)[r0 + i], false);
+            if (h == 0) t = pol.aop(p, t);
+            const uint32_t cnt = p.c + h;  // rank + 1 of the segment
+            if (cnt > 0) static_cast<out_t*>(sargs.rank_out)[cnt - 1] = t.v;
           }
-        }
-        uint32_t hb_next = 0;
-        in_t xn[V];
-        if constexpr (REDUCE) hb_next = load_row_chunk(s, r0, base, valid, bulk, xn);
-        // a full tile that is not the array's last: no element is past the end
-        const bool interior = valid == TILE && base + uint64_t(TILE) < n;
+          // the stage was written through the generic proxy; the producer's
+          // next bulk copy into it is an async-proxy write
+          ptx::fence_proxy_async_smem();
+        } else {
+          // a thread-serial chain per row
 #pragma unroll
-        for (int c = 0; c < CH; ++c) {
-          in_t x[V];
-          uint32_t hb;
-          if constexpr (REDUCE) {
-#pragma unroll
-            for (int j = 0; j < V; ++j) x[j] = xn[j];
-            hb = hb_next;
-            if (c + 1 < CH) hb_next = load_row_chunk(s, r0 + (c + 1) * V, base, valid, bulk, xn);
-          } else {
-            hb = load_row_chunk(s, r0 + c * V, base, valid, bulk, x);
-          }
-          const int e0 = r0 + c * V;
-          union {
-            vec_t u;
-            out_t v[V];
-          } o;
-          // reduce: bit j set when element e0 + j ends its segment (the next
-          // element is a head, or it is the array's last element)
-          uint32_t ends = 0;
-          if constexpr (REDUCE) {
-            ends = (hb >> 1) | ((c + 1 < CH ? (hb_next & 1u) : uint32_t(next_head_after_row)) << (V - 1));
-            if (!interior) {
-#pragma unroll
-              for (int j = 0; j < V; ++j) {
-                const int e = e0 + j;
-                if (e >= valid)
-                  ends &= ~(1u << j);
-                else if (base + uint64_t(e) + 1 >= n)
-                  ends |= 1u << j;
-              }
-            }
-          }
-          if (!SKIP || __any_sync(kFullMask, (hb | ends) != 0u)) {
+          for (int c = 0; c < CH; ++c) {
+            in_t x[V];
+            const uint32_t hb = load_row_chunk(s, r0 + c * V, base, valid, bulk, x);
+            const int e0 = r0 + c * V;
+            union {
+              vec_t u;
+              out_t v[V];
+            } o;
 #pragma unroll
             for (int j = 0; j < V; ++j) {
               const bool head = (hb >> j) & 1u;
               const acc_t before = p;
               p = pol.aop(p, pol.load(x[j], head));
-              if constexpr (!REDUCE) {
-                o.v[j] = excl_kind ? (head ? pol.aid().v : before.v) : p.v;
-              } else {
-                if (((ends >> j) & 1u) && p.c > 0) static_cast<out_t*>(sargs.rank_out)[p.c - 1] = p.v;
-              }
+              o.v[j] = excl_kind ? (head ? pol.aid().v : before.v) : p.v;
             }
-          } else {
-            // no head and no segment end in any of the warp's chunks: the
-            // same chain with those bits known to be zero
-#pragma unroll
-            for (int j = 0; j < V; ++j) {
-              if constexpr (REDUCE) {
-                p = pol.aop(p, pol.load(x[j], false));
-              } else {
-                const acc_t before = p;
-                p = pol.aop(p, pol.load(x[j], false));
-                o.v[j] = excl_kind ? before.v : p.v;
-              }
-            }
+            *reinterpret_cast<vec_t*>(stage + size_t(e0) * sizeof(in_t)) = o.u;
           }
-          if constexpr (!REDUCE) *reinterpret_cast<vec_t*>(stage + size_t(e0) * sizeof(in_t)) = o.u;
-        }
-        if constexpr (BS == 2) {
-          // a full tile with an aligned output leaves by the store warp's bulk copy
-          if ((reinterpret_cast<uintptr_t>(gout) & 15u) == 0 && valid == TILE) ptx::fence_proxy_async_smem();
-        }
-        if (!REDUCE && (BS != 2 || (reinterpret_cast<uintptr_t>(gout) & 15u) != 0 || valid != TILE)) {
-          __syncwarp();
+          if (BS == 2 && (reinterpret_cast<uintptr_t>(gout) & 15u) == 0 && valid == TILE) {
+            // a full tile with an aligned output leaves by the store warp's bulk copy
+            ptx::fence_proxy_async_smem();
+          } else {
+            __syncwarp();
 #pragma unroll
-          for (int c = 0; c < CH; ++c) {
-            const int e0 = w * Cfg::SEG + (c * 32 + lane) * V;
-            union {
-              vec_t u;
-              out_t v[V];
-            } o;
-            o.u = *reinterpret_cast<const vec_t*>(stage + size_t(e0) * sizeof(in_t));
-            if (e0 + V <= valid) {
-              ptx::st_stream<VB>(gout + base + e0, &o.u);
-            } else {
+            for (int c = 0; c < CH; ++c) {
+              const int e0 = w * Cfg::SEG + (c * 32 + lane) * V;
+              union {
+                vec_t u;
+                out_t v[V];
+              } o;
+              o.u = *reinterpret_cast<const vec_t*>(stage + size_t(e0) * sizeof(in_t));
+              if (e0 + V <= valid) {
+                ptx::st_stream<VB>(gout + base + e0, &o.u);
+              } else {
 #pragma unroll
-              for (int j = 0; j < V; ++j)
-                if (e0 + j < valid) gout[base + e0 + j] = o.v[j];
+                for (int j = 0; j < V; ++j)
+                  if (e0 + j < valid) gout[base + e0 + j] = o.v[j];
+              }
             }
+            // the stage was written through the generic proxy; the next bulk
+            // copy into it is an async-proxy write
+            ptx::fence_proxy_async_smem();
           }
         }
       } else {
