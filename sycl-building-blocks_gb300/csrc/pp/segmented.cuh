@@ -22,11 +22,14 @@
 // the last to the first and mirror the element order inside each tile; they
 // are provided for uniform segments.
 //
-// Segmented reduce reuses the same pass without writing the scanned array:
-// the element that ends a non-empty segment writes the segment's value to
-// rank_out[count - 1] (its rank among the non-empty segments: a store with no
-// load in front of it), and segment_gather_kernel moves the totals to their
-// segments; empty segments get the identity from the pre-pass.
+// Segmented reduce writes no scanned array: the element that ends a
+// non-empty segment writes the segment's value to rank_out[count - 1] (its
+// rank among the non-empty segments: a store with no load in front of it),
+// and segment_gather_kernel moves the totals to their segments; empty
+// segments get the identity from the pre-pass. In the rows layout it reads
+// the data once: the reduce pass leaves each row's running value at the
+// row's segment ends and keeps the row's head and end bits, and once the
+// tile's prefix is known only the end elements are read again.
 #pragma once
 
 #include <cstdint>
