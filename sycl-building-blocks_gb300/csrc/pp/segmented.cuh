@@ -132,8 +132,10 @@ struct SegCfg {
 // SKIP (rows layout): a warp whose chunks hold no segment head (and, in the
 // second pass of a reduction, no segment end) combines them without the
 // per-element head tests; it pays off when segments are long.
+// Trace: instrumentation hook with the events of the plain staged kernel
+// (kTr*); the default records nothing and compiles away.
 template <class Pol, int NC, int CH, int STAGES, int LBW, class Heads, bool REVERSE, bool REDUCE, int VB = 16,
-          int LAY = 0, int BS = 0, bool SKIP = false>
+          int LAY = 0, int BS = 0, bool SKIP = false, class Trace = NoTrace>
 __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmented_staged_kernel(const SegArgs sargs) {
   using Cfg = SegCfg<Pol, NC, CH, STAGES, LBW, VB, LAY, (BS == 2 ? 1 : 0)>;
   static_assert(LAY == 0 || (!REVERSE && Heads::kBitmap), "rows: forward scans over CSR heads");
@@ -168,6 +170,11 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
   auto s_rows = [&](int s) { return reinterpret_cast<acc_t*>(meta(s) + Cfg::META_ROWS); };
 
   const Pol pol{};
+  const Trace trace{};
+  // timestamps are read only when a recording Trace is compiled in
+  auto trace_now = [&](int ev, long long tile) {
+    if constexpr (Trace::kOn) trace(ev, tile, ptx::globaltimer_ns());
+  };
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const uint64_t n = args.n;
@@ -201,6 +208,8 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
       // order in which tiles reach their reduce pass
       for (int k = 0;; ++k) {
         const int s = k % STAGES;
+        // traced: the ticket slot holds when the wait for a free stage began
+        const unsigned long long tfree = Trace::kOn ? ptx::globaltimer_ns() : 0ull;
         if (k >= STAGES) {
           if (!mbar_wait_bounded(&empty[s], ((k / STAGES) - 1) & 1, hdr, tmo, 0ull)) break;
           pending &= ~(1u << s);
@@ -208,6 +217,8 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
         const long long t = (long long)atomicAdd(&hdr->ticket, 1ull);
         *s_tile(s) = t;
         if (t < ntiles) {
+          trace(kTrTicket, t, tfree);
+          trace_now(kTrIssue, t);
           const uint64_t base = uint64_t(phys(t)) * TILE;
           const uint64_t valid = (n - base < uint64_t(TILE)) ? (n - base) : uint64_t(TILE);
           const uint32_t bytes = uint32_t(valid * sizeof(in_t)) & ~15u;
@@ -243,13 +254,19 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
       if (!mbar_wait_bounded(&full[s], par, hdr, tmo, 0ull)) break;
       const long long tile = *s_tile(s);
       if (tile >= ntiles) break;
+      if (lane == 0) trace_now(kTrFull, tile);
       // exclusive prefix from the predecessors' descriptors while the compute
       // warps still reduce this tile (two polls in flight, 250 ns apart)
       carry_t excl = pol.cid();
       unsigned long long stats = 0;
       if (tile > 0 && !lookback_pipelined<Pol, LBW, 250u>(pol, args.desc, tile, etag, hdr, tmo, lane, excl, stats))
         break;
+      if (lane == 0) {
+        trace_now(kTrLbDone, tile);
+        trace(kTrLbRounds, tile, stats);
+      }
       if (!mbar_wait_bounded(&aggb[s], par, hdr, tmo, 0ull)) break;
+      if (lane == 0) trace_now(kTrAgg, tile);
       if (tile > 0 && lane == 0)
         codec::publish(args.desc + tile * codec::W, pol.cop(excl, *s_tagg(s)), make_tag(etag, kPrefix));
       if (lane == 0) {
@@ -422,12 +439,17 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
     uint32_t row_heads = 0, row_ends = 0;
     auto reduce_pass = [&](int k) -> bool {
       const int s = k % STAGES;
+      const unsigned long long tw = Trace::kOn ? ptx::globaltimer_ns() : 0ull;
       if (!mbar_wait_bounded(&full[s], (k / STAGES) & 1, hdr, tmo, 0ull)) return false;
       long long tile;
       uint64_t base, mt;
       int valid, bulk;
       tile_geom(s, tile, base, valid, bulk, mt);
       if (tile >= ntiles) return false;
+      if (w == 0 && lane == 0) {
+        trace(kTrRWait, tile, tw);
+        trace_now(kTrRGot, tile);
+      }
       acc_t r = pol.aid();
       if constexpr (LAY == 2) {
         // this lane's row in order; the scan of the (value, count) row totals
@@ -510,6 +532,7 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
           *s_tagg(s) = agg;
           *s_cnt(s) = 0u;
           codec::publish(args.desc + tile * codec::W, agg, make_tag(etag, tile == 0 ? kPrefix : kAggregate));
+          trace_now(kTrAggPub, tile);
         }
       }
       __syncwarp();
@@ -523,11 +546,14 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
       const uint32_t cur_heads = row_heads, cur_ends = row_ends;  // tile k
       const bool have_next = reduce_pass(k + 1);
       const int s = k % STAGES;
+      if constexpr (Trace::kOn)
+        if (w == 0 && lane == 0) trace_now(kTrPWait, *s_tile(s));
       if (!mbar_wait_bounded(&prefb[s], (k / STAGES) & 1, hdr, tmo, 0ull)) break;
       long long tile;
       uint64_t base, mt;
       int valid, bulk;
       tile_geom(s, tile, base, valid, bulk, mt);
+      if (w == 0 && lane == 0) trace_now(kTrSStart, tile);
       const acc_t pw = w == 0 ? *s_pref(s) : pol.aop(*s_pref(s), s_aggs(s)[w]);
       if constexpr (LAY == 2) {
         unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
@@ -679,7 +705,10 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
       }
       }
       __syncwarp();
-      if (lane == 0) ptx::mbar_arrive(BS == 2 ? &scanned[s] : &empty[s]);
+      if (lane == 0) {
+        if (w == 0) trace_now(kTrSDone, tile);
+        ptx::mbar_arrive(BS == 2 ? &scanned[s] : &empty[s]);
+      }
       have = have_next;
     }
   }

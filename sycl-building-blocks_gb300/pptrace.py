@@ -1,4 +1,5 @@
-"""Per-tile timelines of the staged decoupled look-back scan.
+"""Per-tile timelines of the staged decoupled look-back scan and of the
+batched segmented scan / reduce.
 
 Compiles tune/tile_trace.cu (the library's own kernel configuration for one
 scan policy, built with a recording trace hook), runs one traced launch on the
@@ -8,6 +9,10 @@ left out), plus the median tile period of a CTA:
 
     python sycl-building-blocks_gb300/pptrace.py u32 32            # 2^32 input bytes
     python sycl-building-blocks_gb300/pptrace.py f32_compensated 32 --keep trace.bin
+    python sycl-building-blocks_gb300/pptrace.py seg_i32_reduce 30  # log-uniform segments
+
+For the seg_* policies the ticket event holds when the producer began to wait
+for a free stage, and the "scan pass" of a reduction is its totals pass.
 
 Events per tile (16 words; %globaltimer in ns unless noted): 0 data in (seen by
 the look-back warp), 1 aggregate published, 2 aggregate seen by the look-back
@@ -87,7 +92,8 @@ def summarise(raw: np.ndarray) -> dict:
 
 def main() -> int:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("policy", choices=["u32", "f32", "u64", "f64", "f32_compensated", "f32_fp64_carry"])
+    ap.add_argument("policy", choices=["u32", "f32", "u64", "f64", "f32_compensated", "f32_fp64_carry", "seg_i32",
+                                       "seg_f32", "seg_i32_reduce", "seg_f32_reduce"])
     ap.add_argument("log2_bytes", type=int, help="log2 of the input size in bytes (12..34)")
     ap.add_argument("--keep", type=Path, help="also keep the raw per-tile words in this file")
     args = ap.parse_args()
