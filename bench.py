@@ -504,7 +504,8 @@ def bench_segmented(torch, pp, stream, steps) -> dict:
     """65,536 segments, lengths floor(exp(U[0, ln 2^16])) clipped to [1, 2^16]
     (about 2^28 elements), int64 offsets; int32 U[0,1000) and f32 N(0,1)
     payloads. One batched launch in a CUDA graph vs one launch per segment
-    (also replayed from a CUDA graph)."""
+    (also replayed from a CUDA graph), and the batched reduction of the same
+    segments."""
     S = 65536
     g = torch.Generator(device="cpu").manual_seed(0x5EC)
     lens = torch.floor(torch.exp(torch.rand(S, generator=g, dtype=torch.float64) * math.log(2 ** 16)))
@@ -550,12 +551,29 @@ def bench_segmented(torch, pp, stream, steps) -> dict:
                     pp.decoupled_scan_device("inclusive", "plus", x.data_ptr() + a * esz, y.data_ptr() + a * esz,
                                              b - a, dt, stream=s.cuda_stream)
         ms_p, _ = time_device(torch, graph2.replay, max(2, steps // 20), 1, torch.cuda.current_stream())
+        # the batched reduction of the same segments (plain launches on s); n * 4 bytes read per call
+        try:
+            tot = torch.empty(S, dtype=x.dtype, device="cuda")
+            ms_r, _ = time_device(torch, lambda: pp.segmented_reduce("plus", x.data_ptr(), n, d_off.data_ptr(), S,
+                                                                      tot.data_ptr(), dt, stream=s.cuda_stream),
+                                  steps, 3, s)
+            ok_r = True
+            for k in (0, 1, S // 2, S - 1):
+                a, b = int(offs[k]), int(offs[k + 1])
+                ref = float(x[a:b].double().sum().item())
+                ok_r &= abs(float(tot[k].double().item()) - ref) <= 1e-4 * (1 + abs(ref))
+            red = {"batched_ms": round(ms_r / steps, 4), "batched_gbs": round(n * 4 / (ms_r / steps * 1e-3) / 1e9, 2),
+                   "spot_check": bool(ok_r)}
+            del tot
+        except Exception as e:  # the scan figures stand on their own
+            red = {"error": f"{type(e).__name__}: {e}"}
         if pp.stream_status(s.cuda_stream) != 0:
             raise RuntimeError("device error in segmented benchmark")
         res[dt] = {"batched_elems_per_s": round(n * steps / (ms_b * 1e-3), 1), "batched_ms": round(ms_b / steps, 4),
                    "per_segment_launches_ms": round(ms_p / max(2, steps // 20), 3),
                    "speedup": round((ms_p / max(2, steps // 20)) / (ms_b / steps), 2),
-                   "batched_gbs": round(2 * n * 4 / (ms_b / steps * 1e-3) / 1e9, 2), "spot_check": ok}
+                   "batched_gbs": round(2 * n * 4 / (ms_b / steps * 1e-3) / 1e9, 2), "spot_check": ok,
+                   "reduce": red}
         del graph, graph2, x, y
     return res
 
