@@ -73,6 +73,56 @@ def test_segmented_reduce(pp, oracle, cuda, dtype, op, count, max_len):
     lens[0] = 0
     lens[-1] = 0
     lens[10] = 50000
+    _reduce_and_check(pp, oracle, cuda, dtype, op, lens)
+
+
+def _tile_aligned_lengths(kind):
+    """Segment lengths whose starts fall on multiples of 8,064 elements: the
+    tile of the 8-byte payloads' variants; every second multiple is a tile
+    boundary of the 4-byte payloads' (16,128 elements). Segments end on the
+    last element of a tile, start on the first of the next, are one element
+    long on either side of a boundary, and empty ones sit on boundaries."""
+    b = 8064
+    blocks = {
+        "long": [[b], [b - 1, 1], [1, b - 1], [b // 2, b // 2], [0, b, 0], [2 * b], [3, b - 3]],
+        "short": [[5] * 1612 + [4], [1] * 64 + [b - 64], [b - 1, 1], [0, 1, 0, b - 1]],
+    }[kind]
+    lens = []
+    for _ in range(3):
+        for blk in blocks:
+            lens += blk
+    return np.array(lens, dtype=np.int64)
+
+
+@pytest.mark.parametrize("dtype", ["i32", "f32", "u64", "f64"])
+@pytest.mark.parametrize("op", ["plus", "maximum"])
+@pytest.mark.parametrize("kind", ["long", "short"])  # mean lengths about 5,000 and 19
+def test_segmented_reduce_heads_on_tile_boundaries(pp, oracle, cuda, dtype, op, kind):
+    _reduce_and_check(pp, oracle, cuda, dtype, op, _tile_aligned_lengths(kind))
+
+
+@pytest.mark.parametrize("dtype", ["i32", "f32", "u64", "f64"])
+@pytest.mark.parametrize("kind", ["long", "short"])
+def test_segmented_scan_heads_on_tile_boundaries(pp, oracle, cuda, dtype, kind):
+    lens = _tile_aligned_lengths(kind)
+    off = _offsets(lens)
+    n = int(off[-1])
+    x = make_input(dtype, "plus", n, seed=5 * n)
+    d_in, d_off = to_dev(cuda, x), cuda.from_numpy(off).cuda()
+    d_out = cuda.empty_like(d_in)
+    s = cuda.cuda.current_stream().cuda_stream
+    for excl in (False, True):
+        pp.segmented_scan("exclusive" if excl else "inclusive", "plus", d_in.data_ptr(), d_out.data_ptr(), n,
+                          d_off.data_ptr(), lens.size, dtype, stream=s)
+        assert pp.stream_status(s) == 0
+        got = from_dev(d_out, NP[dtype])
+        for k in range(lens.size):
+            a, b = off[k], off[k + 1]
+            if b > a:
+                _check_segment(got[a:b], x[a:b], dtype, "plus", excl, oracle)
+
+
+def _reduce_and_check(pp, oracle, cuda, dtype, op, lens):
     off = _offsets(lens)
     n = int(off[-1])
     x = make_input(dtype, op, n, seed=3 * n)
