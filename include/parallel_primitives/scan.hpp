@@ -6,6 +6,10 @@
 #pragma once
 
 #include "scan_decoupled_lookback.hpp"
+#include "../usm_smart_ptr.hpp"
+
+// as the reference's scan.hpp:27: usm_unique_ptr / alloc for its callers
+using namespace usm_smart_ptr;
 
 namespace parallel_primitives {
 

@@ -4,6 +4,11 @@
 #pragma once
 
 #include "common.hpp"
+#include "../usm_smart_ptr.hpp"
+
+// as the reference's scan_cooperative.hpp:27: usm_unique_ptr / alloc for its
+// callers
+using namespace usm_smart_ptr;
 
 namespace parallel_primitives {
 

@@ -186,6 +186,8 @@ def ref_lib():
         L.ref_brev64.restype = C.c_uint64
         L.ref_upsample.argtypes = [C.c_uint8] * 4
         L.ref_upsample.restype = C.c_uint32
+        L.ref_byte_bit.argtypes = [i32, i32, C.c_uint64, C.c_uint32, C.c_uint32]
+        L.ref_byte_bit.restype = C.c_uint64
         L.ref_num_groups.restype = i32
         _ref = L
     return _ref

@@ -127,4 +127,41 @@ uint32_t ref_funnelshift_r(uint32_t lo, uint32_t hi, uint32_t shift) { return sy
 uint32_t ref_brev32(uint32_t x) { return sycl::ext::brev32(x); }
 uint64_t ref_brev64(uint64_t x) { return sycl::ext::brev64(x); }
 uint32_t ref_upsample(uint8_t a, uint8_t b, uint8_t c, uint8_t d) { return sycl::ext::upsample<uint8_t>(a, b, c, d); }
+
+// Byte / bit helpers (intrinsics.hpp:150-202) on unsigned words of `width`
+// bytes (1, 2, 4 or 8), the word passed and returned zero-extended to 64 bits.
+// op: 0 get_byte(word, a), 1 set_byte(word, byte b, a), 2 set_bit_in_word<b>(word, a),
+//     3 set_bit_in_word(word, a, bool b), 4 read_bit(word, a), 5 flip_bit(word, a).
+uint64_t ref_byte_bit(int op, int width, uint64_t word, uint32_t a, uint32_t b) {
+  auto run = [&]<class T>(T w) -> uint64_t {
+    switch (op) {
+      case 0:
+        return sycl::ext::get_byte<T>(w, a);
+      case 1:
+        return sycl::ext::set_byte<T>(w, uint8_t(b), a);
+      case 2:
+        return b ? sycl::ext::set_bit_in_word<true, T>(w, a) : sycl::ext::set_bit_in_word<false, T>(w, a);
+      case 3:
+        return sycl::ext::set_bit_in_word<T>(w, a, b != 0);
+      case 4:
+        return sycl::ext::read_bit<T>(w, a) ? 1u : 0u;
+      case 5:
+        return sycl::ext::flip_bit<T>(w, a);
+      default:
+        return ~uint64_t(0);
+    }
+  };
+  switch (width) {
+    case 1:
+      return run(uint8_t(word));
+    case 2:
+      return run(uint16_t(word));
+    case 4:
+      return run(uint32_t(word));
+    case 8:
+      return run(uint64_t(word));
+    default:
+      return ~uint64_t(0);
+  }
+}
 }

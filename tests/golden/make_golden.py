@@ -12,6 +12,12 @@ parameters: element i of stream `seed` is mix64(seed + (i + 1) *
 lo + ((x >> 32) * (hi - lo) >> 32) for 32-bit values and
 lo + ((x * (hi - lo)) >> 64) for 64-bit values (oracle/oracle.c).
 
+A second file, tests/golden/intrinsics_bytes_bits.json, holds the
+reference's byte / bit helpers (include/intrinsics.hpp:150-202: get_byte,
+set_byte, both set_bit_in_word overloads, read_bit, flip_bit) evaluated on
+words of 1, 2, 4 and 8 bytes at every byte / bit position (see
+byte_bit_cases()).
+
 Usage:  python tests/golden/make_golden.py
 """
 
@@ -36,6 +42,38 @@ def gen(dtype: str, n: int, seed: int, lo: int, hi: int) -> np.ndarray:
     if dtype in ("u32", "i32"):
         return pyoracle.gen_u32(seed, n, lo, hi).view(NP[dtype])
     return pyoracle.gen_u64(seed, n, lo, hi).view(NP[dtype])
+
+
+BYTE_VALUES = [0x00, 0x5A, 0xFF]
+
+
+def byte_bit_words(width: int) -> list[int]:
+    """Operand words of one width: zero, all ones, an alternating pattern and
+    two splitmix64 words, truncated to the width."""
+    mask = (1 << (8 * width)) - 1
+    return [0, mask, 0xA5C3_0F96_5A3C_F069 & mask, pyoracle.lib().splitmix64(width) & mask,
+            pyoracle.lib().splitmix64(100 + width) & mask]
+
+
+def byte_bit_cases(ref) -> list[dict]:
+    """Every helper at every position of every operand word; per word the
+    results are lists indexed by position (bytes, or bits)."""
+    out = []
+    for width in (1, 2, 4, 8):
+        for w in byte_bit_words(width):
+            e = {"width": width, "word": w,
+                 "get_byte": [int(ref.ref_byte_bit(0, width, w, p, 0)) for p in range(width)],
+                 "set_byte": {str(b): [int(ref.ref_byte_bit(1, width, w, p, b)) for p in range(width)]
+                              for b in BYTE_VALUES}}
+            bits = range(8 * width)
+            e["set_bit_true"] = [int(ref.ref_byte_bit(2, width, w, i, 1)) for i in bits]
+            e["set_bit_false"] = [int(ref.ref_byte_bit(2, width, w, i, 0)) for i in bits]
+            e["set_bit_runtime_true"] = [int(ref.ref_byte_bit(3, width, w, i, 1)) for i in bits]
+            e["set_bit_runtime_false"] = [int(ref.ref_byte_bit(3, width, w, i, 0)) for i in bits]
+            e["read_bit"] = [int(ref.ref_byte_bit(4, width, w, i, 0)) for i in bits]
+            e["flip_bit"] = [int(ref.ref_byte_bit(5, width, w, i, 0)) for i in bits]
+            out.append(e)
+    return out
 
 
 def main() -> None:
@@ -90,6 +128,12 @@ def main() -> None:
     }
     (HERE / "reference_outputs.json").write_text(json.dumps(out, indent=1) + "\n")
     print(f"wrote {len(cases)} scans, {len(reductions)} reductions")
+    bb = {"producer": out["producer"],
+          "ops": "get_byte(word, pos); set_byte(word, byte, pos) per byte value; set_bit_in_word<true|false>(word, "
+                 "idx); set_bit_in_word(word, idx, bool); read_bit(word, idx) as 0/1; flip_bit(word, idx)",
+          "cases": byte_bit_cases(ref)}
+    (HERE / "intrinsics_bytes_bits.json").write_text(json.dumps(bb, separators=(",", ":")) + "\n")
+    print(f"wrote {len(bb['cases'])} byte/bit operand words")
 
 
 if __name__ == "__main__":
