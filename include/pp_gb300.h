@@ -157,7 +157,8 @@ pp_status pp_rows_scan(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype d
 const char* pp_status_string(pp_status status);
 
 /* Synchronises `stream` and returns (then clears) the first device-side
- * error recorded in the stream's cached workspace, or PP_OK. */
+ * error recorded in the stream's cached workspace, else one recorded by
+ * pp_decoupled_scan_device_noalloc on the current device, or PP_OK. */
 pp_status pp_stream_status(pp_stream stream);
 /* Same for a caller-owned workspace. */
 pp_status pp_workspace_status(pp_stream stream, void* d_workspace);
@@ -176,18 +177,19 @@ const char* pp_version(void);
 
 /* ---- allocation-free variant ------------------------------------------------
  * No counterpart in the reference. The same decoupled look-back scan as
- * pp_decoupled_scan_device, for callers that cannot allocate device memory
- * when they scan (inside CUDA-graph capture, in loops that must stay out of
- * the allocator, in plug-ins whose host framework owns all device memory).
- * Its scratch is a fixed 1 MiB array in the library's device image instead
- * of a cudaMalloc'd or per-stream cached workspace, so it allocates nothing.
- * Limit: n up to 1,870,659,581 elements of a 4-byte integer type,
+ * pp_decoupled_scan_device, for callers that must not allocate device memory
+ * when they scan: latency-critical loops that must stay out of the allocator
+ * (whose calls can synchronise the device), plug-ins whose host framework owns
+ * all device memory through its own pool, processes whose device-memory budget
+ * is spent. Its scratch is a fixed 1 MiB array in the library's device image
+ * instead of a cudaMalloc'd or per-stream cached workspace, so it allocates
+ * nothing. Limit: n up to 1,870,659,581 elements of a 4-byte integer type,
  * 2,104,492,029 floats, 511,508,479 elements of an 8-byte integer type or
  * 460,357,631 doubles; larger n returns PP_ERR_WORKSPACE. All calls share the
  * array: calls that overlap on the GPU race, so order them on one stream.
- * The first call on each device looks up the array's address; make it
- * outside stream capture. Device-side timeouts of this variant are not
- * reported by pp_stream_status(). */
+ * The first call on each device looks up the array's address. A device-side
+ * timeout of a call stays in the array until pp_stream_status() on the calls'
+ * stream returns it. */
 pp_status pp_decoupled_scan_device_noalloc(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dtype,
                                            const void* d_in, void* d_out, uint64_t n);
 

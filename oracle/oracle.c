@@ -489,6 +489,84 @@ double oracle_sum_fp64(int dtype, const void* in, uint64_t n) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* 1b/2b. batched segments: the definitions above applied to every segment   */
+/* [offsets[s], offsets[s+1]) in turn (segments split over threads).          */
+
+typedef struct {
+  const type_op_entry* e;
+  int dtype, exclusive, fp64;
+  const unsigned char* in;
+  unsigned char* out;
+  const int64_t* off;
+} seg_ctx;
+
+static void seg_scan_range(void* p, uint64_t b, uint64_t e) {
+  seg_ctx* c = (seg_ctx*)p;
+  for (uint64_t k = b; k < e; ++k) {
+    const uint64_t a = (uint64_t)c->off[k], len = (uint64_t)(c->off[k + 1] - c->off[k]);
+    if (len == 0) continue;
+    if (c->fp64) {
+      const size_t es = c->dtype == 4 ? 4 : 8;
+      oracle_scan_fp64(c->dtype, c->exclusive, c->in + a * es, (double*)c->out + a, len);
+    } else {
+      c->e->seqscan(c->in + a * c->e->size, c->out + a * c->e->size, len, c->exclusive);
+    }
+  }
+}
+
+static int offsets_ok(const int64_t* off, uint64_t n, uint64_t num_segments) {
+  if (off[0] != 0 || (uint64_t)off[num_segments] != n) return 0;
+  for (uint64_t k = 0; k < num_segments; ++k)
+    if (off[k + 1] < off[k]) return 0;
+  return 1;
+}
+
+int oracle_segmented_scan(int dtype, int op, int exclusive, const void* in, void* out, uint64_t n,
+                          const int64_t* offsets, uint64_t num_segments, int threads) {
+  const type_op_entry* e = lookup(dtype, op);
+  if (!e || !offsets_ok(offsets, n, num_segments)) return -1;
+  seg_ctx c = {e, dtype, exclusive, 0, (const unsigned char*)in, (unsigned char*)out, offsets};
+  parallel_ranges(num_segments, threads, seg_scan_range, &c);
+  return 0;
+}
+
+int oracle_segmented_scan_fp64(int dtype, int exclusive, const void* in, double* out, uint64_t n,
+                               const int64_t* offsets, uint64_t num_segments, int threads) {
+  if ((dtype != 4 && dtype != 5) || !offsets_ok(offsets, n, num_segments)) return -1;
+  seg_ctx c = {NULL, dtype, exclusive, 1, (const unsigned char*)in, (unsigned char*)out, offsets};
+  parallel_ranges(num_segments, threads, seg_scan_range, &c);
+  return 0;
+}
+
+static void seg_reduce_range(void* p, uint64_t b, uint64_t e) {
+  seg_ctx* c = (seg_ctx*)p;
+  for (uint64_t k = b; k < e; ++k) {
+    const uint64_t a = (uint64_t)c->off[k], len = (uint64_t)(c->off[k + 1] - c->off[k]);
+    if (c->fp64)
+      ((double*)c->out)[k] = oracle_sum_fp64(c->dtype, c->in + a * (c->dtype == 4 ? 4 : 8), len);
+    else /* an empty segment reduces to the identity */
+      c->e->seqreduce(c->in + a * c->e->size, len, c->out + k * c->e->size);
+  }
+}
+
+int oracle_segmented_reduce(int dtype, int op, const void* in, uint64_t n, const int64_t* offsets,
+                            uint64_t num_segments, void* out, int threads) {
+  const type_op_entry* e = lookup(dtype, op);
+  if (!e || !offsets_ok(offsets, n, num_segments)) return -1;
+  seg_ctx c = {e, dtype, 0, 0, (const unsigned char*)in, (unsigned char*)out, offsets};
+  parallel_ranges(num_segments, threads, seg_reduce_range, &c);
+  return 0;
+}
+
+int oracle_segmented_sum_fp64(int dtype, const void* in, uint64_t n, const int64_t* offsets, uint64_t num_segments,
+                              double* out, int threads) {
+  if ((dtype != 4 && dtype != 5) || !offsets_ok(offsets, n, num_segments)) return -1;
+  seg_ctx c = {NULL, dtype, 0, 1, (const unsigned char*)in, (unsigned char*)out, offsets};
+  parallel_ranges(num_segments, threads, seg_reduce_range, &c);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* 3. reference algorithms on CPU threads                                    */
 
 int oracle_ref_decoupled_scan(int dtype, int op, int exclusive, const void* in, void* out, uint64_t n, int threads,

@@ -41,6 +41,19 @@ int oracle_reduce(int dtype, int op, const void* in, uint64_t n, void* result);
 int oracle_scan_fp64(int dtype, int exclusive, const void* in, double* out, uint64_t n);
 double oracle_sum_fp64(int dtype, const void* in, uint64_t n);
 
+/* Batched segments (CSR int64 offsets, offsets[0] = 0, offsets[S] = n,
+ * nondecreasing): the exact scan / reduction above, and the FP64 oracles,
+ * applied to each segment on its own; an empty segment reduces to the
+ * operator's identity. -1 for an unsupported (dtype, op) or bad offsets. */
+int oracle_segmented_scan(int dtype, int op, int exclusive, const void* in, void* out, uint64_t n,
+                          const int64_t* offsets, uint64_t num_segments, int threads);
+int oracle_segmented_scan_fp64(int dtype, int exclusive, const void* in, double* out, uint64_t n,
+                               const int64_t* offsets, uint64_t num_segments, int threads);
+int oracle_segmented_reduce(int dtype, int op, const void* in, uint64_t n, const int64_t* offsets,
+                            uint64_t num_segments, void* out, int threads);
+int oracle_segmented_sum_fp64(int dtype, const void* in, uint64_t n, const int64_t* offsets, uint64_t num_segments,
+                              double* out, int threads);
+
 /* 3. reference algorithms on `threads` CPU threads (0 = all cores).
  * local_mem_bytes sets the partition length as the reference derives it from
  * the device's local memory size (scan_decoupled_lookback.hpp:108-112).

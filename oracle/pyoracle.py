@@ -43,6 +43,10 @@ def lib() -> C.CDLL:
         L.oracle_fnv1a64.argtypes = [vp, u64]
         L.oracle_fnv1a64.restype = u64
         L.oracle_num_threads.restype = i32
+        L.oracle_segmented_scan.argtypes = [i32, i32, i32, vp, vp, u64, vp, u64, i32]
+        L.oracle_segmented_scan_fp64.argtypes = [i32, i32, vp, vp, u64, vp, u64, i32]
+        L.oracle_segmented_reduce.argtypes = [i32, i32, vp, u64, vp, u64, vp, i32]
+        L.oracle_segmented_sum_fp64.argtypes = [i32, vp, u64, vp, u64, vp, i32]
         _lib = L
     return _lib
 
@@ -86,6 +90,55 @@ def scan_fp64(a: np.ndarray, exclusive: bool = False) -> np.ndarray:
 def sum_fp64(a: np.ndarray) -> float:
     a = np.ascontiguousarray(a)
     return float(lib().oracle_sum_fp64(_code(a), _ptr(a), a.size))
+
+
+def _offsets(offsets: np.ndarray, n: int) -> np.ndarray:
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    if off.size < 1 or off[0] != 0 or off[-1] != n:
+        raise ValueError("offsets must start at 0 and end at n")
+    return off
+
+
+def segmented_scan(a: np.ndarray, offsets: np.ndarray, op="plus", exclusive: bool = False,
+                   threads: int = 0) -> np.ndarray:
+    """Exact scan of every segment [offsets[s], offsets[s+1]) on its own."""
+    a = np.ascontiguousarray(a)
+    off = _offsets(offsets, a.size)
+    out = np.empty_like(a)
+    if lib().oracle_segmented_scan(_code(a), _op(op), int(exclusive), _ptr(a), _ptr(out), a.size, _ptr(off),
+                                   off.size - 1, threads) != 0:
+        raise ValueError("unsupported dtype/op or bad offsets")
+    return out
+
+
+def segmented_scan_fp64(a: np.ndarray, offsets: np.ndarray, exclusive: bool = False, threads: int = 0) -> np.ndarray:
+    a = np.ascontiguousarray(a)
+    off = _offsets(offsets, a.size)
+    out = np.empty(a.size, dtype=np.float64)
+    if lib().oracle_segmented_scan_fp64(_code(a), int(exclusive), _ptr(a), _ptr(out), a.size, _ptr(off),
+                                        off.size - 1, threads) != 0:
+        raise ValueError("float inputs only, or bad offsets")
+    return out
+
+
+def segmented_reduce(a: np.ndarray, offsets: np.ndarray, op="plus", threads: int = 0) -> np.ndarray:
+    """Reduction of every segment (the identity for an empty one)."""
+    a = np.ascontiguousarray(a)
+    off = _offsets(offsets, a.size)
+    out = np.empty(off.size - 1, dtype=a.dtype)
+    if lib().oracle_segmented_reduce(_code(a), _op(op), _ptr(a), a.size, _ptr(off), off.size - 1, _ptr(out),
+                                     threads) != 0:
+        raise ValueError("unsupported dtype/op or bad offsets")
+    return out
+
+
+def segmented_sum_fp64(a: np.ndarray, offsets: np.ndarray, threads: int = 0) -> np.ndarray:
+    a = np.ascontiguousarray(a)
+    off = _offsets(offsets, a.size)
+    out = np.empty(off.size - 1, dtype=np.float64)
+    if lib().oracle_segmented_sum_fp64(_code(a), _ptr(a), a.size, _ptr(off), off.size - 1, _ptr(out), threads) != 0:
+        raise ValueError("float inputs only, or bad offsets")
+    return out
 
 
 def ref_decoupled_scan(a: np.ndarray, op="plus", exclusive=False, threads=0, local_mem_bytes=65536,
@@ -189,6 +242,8 @@ def ref_lib():
         L.ref_byte_bit.argtypes = [i32, i32, C.c_uint64, C.c_uint32, C.c_uint32]
         L.ref_byte_bit.restype = C.c_uint64
         L.ref_num_groups.restype = i32
+        L.ref_decoupled_scan_u32_plus.argtypes = [vp, vp, u64, i32]
+        L.ref_decoupled_scan_u32_plus.restype = i32
         _ref = L
     return _ref
 

@@ -401,7 +401,13 @@ const char* pp_status_string(pp_status status) {
 }
 
 pp_status pp_stream_status(pp_stream stream) {
-  return to_c(pp::host::read_device_error(static_cast<cudaStream_t>(stream), nullptr));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const pp_status st = to_c(pp::host::read_device_error(s, nullptr));
+  if (st != PP_OK) return st;
+  // an error of the allocation-free scan stays in its scratch until read here
+  if (void* scratch = pp::capi::noalloc_scratch_used_on_current_device())
+    return to_c(pp::host::read_device_error(s, scratch));
+  return PP_OK;
 }
 
 pp_status pp_workspace_status(pp_stream stream, void* d_workspace) {

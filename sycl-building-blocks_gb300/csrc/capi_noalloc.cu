@@ -1,14 +1,14 @@
 // Allocation-free variant of the decoupled look-back scan entry point.
 //
-// Who needs it: some callers cannot allocate device memory at the moment they
-// run a scan. Code executing while a CUDA graph is being captured may not
-// call cudaMalloc; latency-critical loops must not enter the allocator, whose
-// calls can synchronise the whole device; and plug-ins hosted by a framework
-// that owns all device memory through its own pool are not allowed to create
-// allocations behind its back. The regular entry points take their scratch
-// (workspace header plus look-back descriptors) from a per-stream cache that
-// grows with cudaMallocAsync, or from a buffer the caller passes in; this one
-// takes it from a fixed array compiled into the library's device image, so it
+// Who needs it: callers that must not allocate device memory at the moment
+// they scan. Latency-critical loops must stay out of the allocator, whose
+// calls can synchronise the whole device; plug-ins hosted by a framework that
+// owns all device memory through its own pool may not create allocations
+// behind its back; and a process whose device-memory budget is already spent
+// still has to scan. The regular entry points take their scratch (workspace
+// header plus look-back descriptors) from a per-stream cache that grows with
+// cudaMallocAsync, or from a buffer the caller passes in; this one takes it
+// from a fixed array compiled into the library's device image, so it
 // allocates nothing at all.
 //
 // Limits and rules:
@@ -24,15 +24,16 @@
 //     exits;
 //   * all calls share the one array, which keeps the last call's contents.
 //     Each call therefore clears the part it uses (cudaMemsetAsync on the
-//     stream, no allocation) before its kernel. Calls that overlap on the GPU
-//     (on different streams, or from different threads without ordering)
-//     race on the array and give wrong results: order them on one stream;
+//     stream, no allocation) before its kernel, all but the sticky error word.
+//     Calls that overlap on the GPU (on different streams, or from different
+//     threads without ordering) race on the array and give wrong results:
+//     order them on one stream;
 //   * the first call on each device looks up the array's device address with
-//     cudaGetSymbolAddress (once per device, with that device current); make
-//     that first call outside any stream capture;
-//   * a device-side timeout is recorded in the shared scratch only and is not
-//     reported by pp_stream_status(); callers that need that status use
-//     pp_scan_ws() with their own workspace.
+//     cudaGetSymbolAddress (once per device, with that device current);
+//   * a device-side timeout is recorded in the array's error word, which the
+//     next call leaves alone; pp_stream_status() on the stream of the calls
+//     returns it (and clears it) after the stream's own workspace errors.
+#include <cstddef>
 #include <cstdint>
 #include <mutex>
 
@@ -70,6 +71,19 @@ pp_status scratch_address(void** out) {
 
 }  // namespace
 
+namespace pp {
+namespace capi {
+// The scratch of the allocation-free variant on the current device, or null
+// when that variant has not run on it.
+void* noalloc_scratch_used_on_current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+  std::lock_guard<std::mutex> g(g_scratch_mu);
+  return g_scratch_addr[dev];
+}
+}  // namespace capi
+}  // namespace pp
+
 extern "C" pp_status pp_decoupled_scan_device_noalloc(pp_stream stream, pp_scan_kind kind, pp_op op,
                                                       pp_dtype dtype, const void* d_in, void* d_out, uint64_t n) {
   if (kind != PP_SCAN_INCLUSIVE && kind != PP_SCAN_EXCLUSIVE) return PP_ERR_INVALID_ARG;
@@ -88,8 +102,13 @@ extern "C" pp_status pp_decoupled_scan_device_noalloc(pp_stream stream, pp_scan_
   st = scratch_address(&scratch);
   if (st != PP_OK) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  // the previous call's header and descriptors must not leak into this one
-  if (cudaMemsetAsync(scratch, 0, need, s) != cudaSuccess) return PP_ERR_CUDA;
+  // the previous call's header and descriptors must not leak into this one;
+  // its error word stays until pp_stream_status() reads it
+  constexpr size_t kErr = offsetof(pp::WsHeader, error);
+  unsigned char* base = static_cast<unsigned char*>(scratch);
+  if (cudaMemsetAsync(base, 0, kErr, s) != cudaSuccess) return PP_ERR_CUDA;
+  if (cudaMemsetAsync(base + kErr + sizeof(unsigned int), 0, need - kErr - sizeof(unsigned int), s) != cudaSuccess)
+    return PP_ERR_CUDA;
 
   pp::capi::ScanReq r;
   r.s = s;

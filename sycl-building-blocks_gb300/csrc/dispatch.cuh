@@ -66,5 +66,9 @@ Status rows_scan_typed(const SegReq& r);
 Status scan_f32_precision(const ScanReq& r, pp_precision prec);
 size_t workspace_f32_precision(pp_scan_algo algo, pp_precision prec, const void* in, const void* out, uint64_t n);
 
+// Scratch array of the allocation-free scan on the current device, or null
+// when that entry point has not run there (capi_noalloc.cu).
+void* noalloc_scratch_used_on_current_device();
+
 }  // namespace capi
 }  // namespace pp

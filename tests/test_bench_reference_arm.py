@@ -16,8 +16,10 @@ ROOT = Path(__file__).resolve().parent.parent
 def _run(extra_env=None):
     env = dict(os.environ)
     env.update(extra_env or {})
+    # a 2^22-element workload keeps the CPU suite quick; the arm scans the whole
+    # workload every step whatever its size
     return subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "2", "--warmup",
-                           "3"], capture_output=True, text=True, cwd=ROOT, env=env, timeout=600)
+                           "3", "--n", str(1 << 22)], capture_output=True, text=True, cwd=ROOT, env=env, timeout=600)
 
 
 def test_reference_arm_prints_the_contract_line():
@@ -34,6 +36,7 @@ def test_reference_arm_prints_the_contract_line():
     cb = line["cpu_baseline"]
     assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["value"] == line["value"]
     assert cb["matches_oracle"] is True
+    assert line["config"]["n"] == 1 << 22 and line["config"]["sample_per_step"] == 1 << 22
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
 

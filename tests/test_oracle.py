@@ -97,3 +97,36 @@ def test_fp64_oracle(oracle):
     y = np.array([1e16, 1.0, -1e16], dtype=np.float64)
     assert oracle.scan_fp64(y)[-1] == 1.0  # compensated for f64 inputs
     assert oracle.sum_fp64(y) == 1.0
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.uint64, np.float32])
+def test_segmented_oracle_is_the_scan_of_each_segment(oracle, dtype):
+    """oracle.segmented_* against the single-array oracle applied to every
+    segment on its own (empty segments included)."""
+    rng = np.random.default_rng(3)
+    lens = rng.integers(0, 40, 500)
+    lens[:3] = 0
+    lens[-1] = 0
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    n = int(off[-1])
+    x = (rng.standard_normal(n) if dtype == np.float32 else rng.integers(0, 1 << 20, n)).astype(dtype)
+    for excl in (False, True):
+        got = oracle.segmented_scan(x, off, "plus", excl)
+        for k in range(lens.size):
+            a, b = off[k], off[k + 1]
+            assert np.array_equal(got[a:b], oracle.scan(x[a:b], "plus", excl))
+    red = oracle.segmented_reduce(x, off, "maximum")
+    for k in range(lens.size):
+        a, b = off[k], off[k + 1]
+        assert red[k] == oracle.reduce(x[a:b], "maximum")  # the identity when empty
+    if dtype == np.float32:
+        f = oracle.segmented_scan_fp64(x, off)
+        t = oracle.segmented_sum_fp64(x, off)
+        for k in range(lens.size):
+            a, b = off[k], off[k + 1]
+            assert np.array_equal(f[a:b], oracle.scan_fp64(x[a:b]))
+            assert t[k] == oracle.sum_fp64(x[a:b])
+    bad = off.copy()
+    bad[-1] = n + 5
+    with pytest.raises(ValueError):
+        oracle.segmented_scan(x, bad, "plus")  # offsets must end at n

@@ -6,7 +6,10 @@ Error measures per prefix i (s = FP64 oracle, g = GPU result):
   rel_i  = |g_i - s_i| / |s_i|, over prefixes with |s_i| >= 1e-3 * rms(s)
            (near-zero crossings of a random walk have no meaningful relative
            error in FP32 output);
-  norm   = max_i |g_i - s_i| / max_i |s_i|.
+  norm   = max_i |g_i - s_i| / max_i |s_i|;
+  abs_i  = |g_i - s_i| / sum_{j<=i} |x_j|, over every prefix, the excluded
+           near-zero ones included: the error against the magnitude the sum
+           was built from.
 """
 
 from __future__ import annotations
@@ -27,6 +30,12 @@ def _errors(got, want):
     return float(rel.max()), float(np.sqrt(np.mean(rel * rel))), float(err.max() / np.abs(want).max())
 
 
+def _abs_errors(got, want, x):
+    """max_i |g_i - s_i| / sum_{j<=i} |x_j| over every prefix."""
+    cabs = np.cumsum(np.abs(x.astype(np.float64)))
+    return float(np.max(np.abs(got.astype(np.float64) - want) / np.maximum(cabs, np.finfo(np.float64).tiny)))
+
+
 def _scan(pp, cuda, x, precision, excl=False, algo="auto"):
     d_in = to_dev(cuda, x)
     d_out = cuda.empty_like(d_in)
@@ -43,10 +52,13 @@ def test_compensated_beats_plain_and_meets_1e6(pp, oracle, cuda, dist):
     x = oracle.gen_f32_normal(21, n) if dist == "normal" else oracle.gen_f32_signed_lognormal(22, n, 0.0, 2.0)
     want = oracle.scan_fp64(x)
     plain = _errors(_scan(pp, cuda, x, "default"), want)
-    comp = _errors(_scan(pp, cuda, x, "compensated"), want)
+    comp_out = _scan(pp, cuda, x, "compensated")
+    comp = _errors(comp_out, want)
     f64c = _errors(_scan(pp, cuda, x, "fp64_carry"), want)
     # compensated: every prefix (away from zero crossings) within 1e-6 relative
     assert comp[0] <= 1e-6, comp
+    # and every prefix, near-zero ones included, within 1e-6 of sum |x_j|
+    assert _abs_errors(comp_out, want, x) <= 1e-6
     assert comp[2] < plain[2] and comp[2] < f64c[2] * 1.01 + 1e-12, (plain, comp, f64c)
     assert f64c[2] <= plain[2] * 1.01, (plain, f64c)
 
