@@ -5,6 +5,10 @@ decoupled look-back inclusive plus-scan of n = 2^30 uint32 values drawn
 uniformly from [0, 2^16), counting 2n*4 bytes (read + write) per scan, with
 the input resident in HBM (4 GiB in + 4 GiB out, far above the 129 MB L2, so
 no flush is needed between steps). A step is one scan over the whole array.
+The input is the splitmix64 stream the oracle, the tests and the CPU baselines
+use (generated on the device with the same formula), and the timed scans'
+output is checked exactly: on the device (neighbouring differences give back
+the input) and, in the CPU-baseline leg, against the oracle's scan.
 
 Also reported:
   roofline      achieved GB/s of the scan kernel (CUDA events around every
@@ -13,8 +17,9 @@ Also reported:
                 (pp_decoupled_scan_host): pinned host input -> device, scan,
                 device -> pinned host output, every step;
   cpu_baseline  the reference's decoupled look-back algorithm restated in C
-                (oracle/oracle.c) on the host cores, on a bounded sample;
-  secondary     the other HBM-scale primitives of the same workload family.
+                (oracle/oracle.c) on all host cores, on the whole input;
+  secondary     the other HBM-scale primitives of the same workload family,
+                each output checked after its timing (`verified`).
 
 `--impl reference` times the reference's CPU algorithm alone (the oracle
 restatement, or the reference headers compiled against the SYCL CPU shim

@@ -171,6 +171,22 @@ pp_status pp_set_max_ctas(int ctas);
 /* Fault injection for tests: the tile with this index never publishes its
  * look-back descriptor, so its successors' waits time out (-1 = off). */
 pp_status pp_debug_set_skip_tile(long long tile);
+/* Descriptor-protocol perturbation for tests (no counterpart in the
+ * reference, whose look-back correctness depends on timing,
+ * partition_descriptor.h:115-130, scan_decoupled_lookback.hpp:143-174):
+ * while max_delay_ns > 0 (at most 1,000,000), every tile of a decoupled scan
+ * delays publishing its aggregate and its inclusive prefix by a pseudo-random
+ * time in [0, max_delay_ns] drawn from (seed, tile), spaces the words of a
+ * multi-word descriptor by up to max_delay_ns / 4, and counts look-back
+ * outcomes (pp_debug_lookback_counters). Every wait stays bounded. 0 = off. */
+pp_status pp_debug_set_lookback_delay(uint32_t max_delay_ns, uint32_t seed);
+/* Synchronises `stream` and returns, then clears, the look-back counters of
+ * its cached workspace gathered while the perturbation was on: [0] tiles
+ * whose nearest predecessor held its inclusive prefix (reduce-then-scan),
+ * [1] tiles that folded published aggregates back to an older prefix
+ * (scan-then-reduce), [2] look-backs over more than 32 predecessors, [3]
+ * polls that met a half-written multi-word descriptor. */
+pp_status pp_debug_lookback_counters(pp_stream stream, uint64_t counters[4]);
 
 /* Library version string. */
 const char* pp_version(void);

@@ -432,6 +432,29 @@ pp_status pp_debug_set_skip_tile(long long tile) {
   return PP_OK;
 }
 
+pp_status pp_debug_set_lookback_delay(uint32_t max_delay_ns, uint32_t seed) {
+  if (max_delay_ns > 1000000u) return PP_ERR_INVALID_ARG;
+  pp::host::settings().debug_seed.store(seed);
+  pp::host::settings().debug_delay_ns.store(max_delay_ns);
+  return PP_OK;
+}
+
+pp_status pp_debug_lookback_counters(pp_stream stream, uint64_t* counters) {
+  if (!counters) return PP_ERR_INVALID_ARG;
+  for (int i = 0; i < 4; ++i) counters[i] = 0;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  void* ws = pp::host::WorkspaceCache::instance().find(s);
+  if (!ws) return to_c(pp::host::from_cuda(cudaStreamSynchronize(s)));
+  unsigned long long* d = static_cast<pp::WsHeader*>(ws)->dbg;
+  unsigned long long h[4] = {0, 0, 0, 0};
+  cudaError_t e = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, sizeof(h), s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return PP_ERR_CUDA;
+  for (int i = 0; i < 4; ++i) counters[i] = h[i];
+  return PP_OK;
+}
+
 namespace {
 Status seg_dispatch(const pp::capi::SegReq& r, pp_dtype dt, int which) {
   using namespace pp::capi;

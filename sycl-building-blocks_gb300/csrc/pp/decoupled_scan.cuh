@@ -56,7 +56,41 @@ struct ScanArgs {
   long long debug_skip_tile;  // a tile that never publishes (timeout tests); -1 = off
   int exclusive;
   int head;  // staged kernel: elements between the previous 16-byte boundary and in[0]
+  // Descriptor perturbation knob of the staged kernel (tests; 0 = off): every
+  // tile delays the publication of its aggregate and of its inclusive prefix
+  // by a pseudo-random time in [0, debug_delay_ns] ns drawn from
+  // (debug_seed, tile), spaces the words of a multi-word descriptor by up to a
+  // quarter of that, and counts look-back outcomes in WsHeader::dbg.
+  uint32_t debug_delay_ns = 0;
+  uint32_t debug_seed = 0;
 };
+
+// Pseudo-random delay in [0, max_ns] for event `ev` of `tile` (a 32-bit
+// integer hash of seed, tile and event).
+__device__ __forceinline__ uint32_t debug_delay(uint32_t seed, long long tile, uint32_t ev, uint32_t max_ns) {
+  uint32_t h = seed ^ (uint32_t(tile) * 0x9E3779B1u) ^ (uint32_t(uint64_t(tile) >> 32) * 0x85EBCA77u) ^
+               (ev * 0xC2B2AE3Du);
+  h ^= h >> 16;
+  h *= 0x7FEB352Du;
+  h ^= h >> 15;
+  h *= 0x846CA68Bu;
+  h ^= h >> 16;
+  return max_ns ? h % (max_ns + 1u) : 0u;
+}
+
+// Publishes descriptor `d` of `tile`; with the perturbation knob on, after a
+// pseudo-random delay and with its words spaced apart (event 0: aggregate,
+// 1: inclusive prefix).
+template <class C>
+__device__ __forceinline__ void publish_desc(const ScanArgs& args, uint64_t* d, const C& v, uint32_t tag,
+                                             long long tile, uint32_t ev) {
+  if (args.debug_delay_ns == 0u) {
+    desc_codec<C>::publish(d, v, tag);
+    return;
+  }
+  ptx::nanosleep(debug_delay(args.debug_seed, tile, ev, args.debug_delay_ns));
+  desc_codec<C>::publish_spaced(d, v, tag, debug_delay(args.debug_seed, tile, ev + 2u, args.debug_delay_ns / 4u));
+}
 
 __host__ __device__ constexpr size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -330,10 +364,15 @@ __device__ __noinline__ EdgeChunk<T, V> load_edge_chunk(const unsigned char* sta
 }
 
 // Warp-wide look-back reading LBW windows of 32 descriptors per round trip.
+// depth_out (optional): tile minus the index of the predecessor whose
+// inclusive prefix ended the look-back (-1 for the identity before tile 0);
+// torn_out (optional): incremented for every poll that met a half-written
+// multi-word descriptor.
 template <class Pol, int LBW>
 __device__ __forceinline__ bool lookback_multi(const Pol& pol, const uint64_t* desc, long long tile,
                                                uint32_t etag, WsHeader* hdr, uint64_t timeout_ns, int lane,
-                                               typename Pol::carry_t& out, unsigned long long& stats) {
+                                               typename Pol::carry_t& out, unsigned long long& stats,
+                                               long long* depth_out = nullptr, unsigned* torn_out = nullptr) {
   unsigned rounds = 0, spin_total = 0;
   using C = typename Pol::carry_t;
   using codec = desc_codec<C>;
@@ -345,13 +384,20 @@ __device__ __forceinline__ bool lookback_multi(const Pol& pol, const uint64_t* d
   while (true) {
     C v[LBW];
     uint32_t st[LBW];
+    bool torn = false;
 #pragma unroll
     for (int j = 0; j < LBW; ++j) {
       const long long t = base - lane - 32 * j;
       v[j] = pol.cid();
       st[j] = kPrefix;
-      if (t >= 0) st[j] = codec::read(desc + t * codec::W, etag, v[j]);
+      if (t >= 0) {
+        uint64_t raw[codec::W];
+        codec::load_raw(desc + t * codec::W, raw);
+        st[j] = codec::decode(raw, etag, v[j]);
+        if (torn_out) torn |= codec::torn(raw, etag);
+      }
     }
+    if (torn_out && __ballot_sync(kFullMask, torn)) ++*torn_out;
     // nearest inclusive prefix: first window with one, lowest lane in it
     int pj = LBW, pl = 32;
     bool blocked = false;
@@ -400,7 +446,10 @@ __device__ __forceinline__ bool lookback_multi(const Pol& pol, const uint64_t* d
         acc = pol.cop(w, acc);
       }
     }
-    if (pj < LBW) break;
+    if (pj < LBW) {
+      if (depth_out) *depth_out = tile - (base - pl - 32 * pj);
+      break;
+    }
     base -= 32 * LBW;
   }
   out = acc;
@@ -414,11 +463,13 @@ __device__ __forceinline__ bool lookback_multi(const Pol& pol, const uint64_t* d
 // round trip. Here a second poll is issued GAP_NS after the first and each
 // evaluated poll is re-issued at once, so successive samples of the window
 // are about half a round trip apart.
+// depth_out / torn_out as for lookback_multi.
 template <class Pol, int LBW, unsigned GAP_NS, bool TIMED = false>
 __device__ __forceinline__ bool lookback_pipelined(const Pol& pol, const uint64_t* desc, long long tile,
                                                    uint32_t etag, WsHeader* hdr, uint64_t timeout_ns, int lane,
                                                    typename Pol::carry_t& out, unsigned long long& stats,
-                                                   unsigned long long* first_rt = nullptr) {
+                                                   unsigned long long* first_rt = nullptr,
+                                                   long long* depth_out = nullptr, unsigned* torn_out = nullptr) {
   using C = typename Pol::carry_t;
   using codec = desc_codec<C>;
   constexpr int W = codec::W;
@@ -440,13 +491,18 @@ __device__ __forceinline__ bool lookback_pipelined(const Pol& pol, const uint64_
   auto step = [&](const uint64_t (&r)[LBW][W]) -> int {
     C v[LBW];
     uint32_t st[LBW];
+    bool torn = false;
 #pragma unroll
     for (int j = 0; j < LBW; ++j) {
       const long long t = base - lane - 32 * j;
       v[j] = pol.cid();
       st[j] = kPrefix;
-      if (t >= 0) st[j] = codec::decode(r[j], etag, v[j]);
+      if (t >= 0) {
+        st[j] = codec::decode(r[j], etag, v[j]);
+        if (torn_out) torn |= codec::torn(r[j], etag);
+      }
     }
+    if (torn_out && __ballot_sync(kFullMask, torn)) ++*torn_out;
     int pj = LBW, pl = 32;
     bool blocked = false;
 #pragma unroll
@@ -475,7 +531,10 @@ __device__ __forceinline__ bool lookback_pipelined(const Pol& pol, const uint64_
         acc = pol.cop(x, acc);
       }
     }
-    if (pj < LBW) return 1;
+    if (pj < LBW) {
+      if (depth_out) *depth_out = tile - (base - pl - 32 * pj);
+      return 1;
+    }
     base -= 32 * LBW;
     return 2;
   };
@@ -667,13 +726,22 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
       if (tile > 0) {
         bool ok;
         unsigned long long rt = 0;
+        const bool dbg = args.debug_delay_ns != 0u;
+        long long depth = 0;
+        unsigned torn = 0;
         if constexpr (PG > 0)
           ok = lookback_pipelined<Pol, LBW, PG, Trace::kOn>(pol, args.desc, tile, etag, hdr, tmo, lane, excl, stats,
-                                                           &rt);
+                                                           &rt, dbg ? &depth : nullptr, dbg ? &torn : nullptr);
         else
-          ok = lookback_multi<Pol, LBW>(pol, args.desc, tile, etag, hdr, tmo, lane, excl, stats);
+          ok = lookback_multi<Pol, LBW>(pol, args.desc, tile, etag, hdr, tmo, lane, excl, stats,
+                                        dbg ? &depth : nullptr, dbg ? &torn : nullptr);
         if (!ok) break;
         trace(kTrPollRt, tile, rt);
+        if (dbg && lane == 0) {
+          atomicAdd(&hdr->dbg[depth == 1 ? 0 : 1], 1ull);
+          if (depth > 32) atomicAdd(&hdr->dbg[2], 1ull);
+          if (torn) atomicAdd(&hdr->dbg[3], (unsigned long long)torn);
+        }
       }
       trace_now(kTrLbDone, tile);
       trace(kTrLbRounds, tile, stats);
@@ -682,7 +750,7 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
       // the tile aggregate was published by the last compute warp of the
       // reduce pass (tile 0: as its inclusive prefix)
       if (tile > 0 && lane == 0 && tile != args.debug_skip_tile)
-        codec::publish(args.desc + tile * codec::W, pol.cop(excl, *s_tagg(s)), make_tag(etag, kPrefix));
+        publish_desc(args, args.desc + tile * codec::W, pol.cop(excl, *s_tagg(s)), make_tag(etag, kPrefix), tile, 1u);
       if (lane == 0) {
         *s_pref(s) = excl;
         ptx::mbar_arrive(&prefb[s]);
@@ -872,7 +940,8 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
           *s_tagg(s) = agg;
           *s_cnt(s) = 0u;
           if (tile != args.debug_skip_tile)
-            codec::publish(args.desc + tile * codec::W, agg, make_tag(etag, tile == 0 ? kPrefix : kAggregate));
+            publish_desc(args, args.desc + tile * codec::W, agg, make_tag(etag, tile == 0 ? kPrefix : kAggregate),
+                         tile, 0u);
           trace_now(kTrAggPub, tile);
         }
       }

@@ -43,6 +43,8 @@ enum class Status : int {
 struct Settings {
   std::atomic<unsigned long long> timeout_ns{1000000000ull};  // every device wait gives up after 1 s
   std::atomic<long long> debug_skip_tile{-1};
+  std::atomic<unsigned> debug_delay_ns{0};  // descriptor perturbation knob (0 = off)
+  std::atomic<unsigned> debug_seed{0};
   std::atomic<int> max_ctas{0};  // 0 = occupancy x SMs
 };
 inline Settings& settings() {
@@ -342,6 +344,8 @@ inline Status decoupled_scan(cudaStream_t s, const void* in, void* out, uint64_t
   a.desc = w.desc;
   a.timeout_ns = settings().timeout_ns.load();
   a.debug_skip_tile = settings().debug_skip_tile.load();
+  a.debug_delay_ns = settings().debug_delay_ns.load();
+  a.debug_seed = settings().debug_seed.load();
   a.exclusive = exclusive ? 1 : 0;
   a.head = 0;
   const int cap = grid_ctas > 0 ? grid_ctas : settings().max_ctas.load();

@@ -107,6 +107,10 @@ struct SegCfg {
   static_assert(TILE % 128 == 0, "tile must cover whole 16-byte bitmap words");
   static constexpr int TILE_BYTES = TILE * int(sizeof(in_t));
   static constexpr int MAP_BYTES = TILE / 8;  // head bits of one tile
+  // a stage's map slot: the tile's head bits and, for reductions, the first
+  // 16 bytes of the next tile's (whether the tile's last element ends its
+  // segment is then known from shared memory)
+  static constexpr int MAP_STRIDE = MAP_BYTES + 16;
   static constexpr int SW = SW_;  // store warps (1: finished tiles leave by one bulk copy, rows scans only)
   static_assert(SW == 0 || (SW == 1 && LAY_ == 2), "the store warp serves the rows layout");
   static constexpr int THREADS = (NC + 2 + SW) * 32;
@@ -120,7 +124,7 @@ struct SegCfg {
   static constexpr size_t META_ROWS = align_up(META_CNT + 4, 16);  // acc_t[NC * 32] row prefixes (LAY 2)
   static constexpr size_t META_BYTES = align_up(META_ROWS + (LAY_ == 2 ? NC_ * 32 * sizeof(acc_t) : 0), 16);
   static constexpr size_t OFF_MAP = size_t(STAGES) * TILE_BYTES;
-  static constexpr size_t OFF_META = OFF_MAP + size_t(STAGES) * MAP_BYTES;
+  static constexpr size_t OFF_META = OFF_MAP + size_t(STAGES) * MAP_STRIDE;
   static constexpr size_t OFF_BAR = align_up(OFF_META + STAGES * META_BYTES, 8);
   static constexpr size_t SMEM = OFF_BAR + 5 * STAGES * 8;  // full, empty, aggb, prefb, scanned
 };
@@ -166,7 +170,7 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
   auto s_tagg = [&](int s) { return reinterpret_cast<carry_t*>(meta(s) + Cfg::META_TAGG); };
   auto s_tile = [&](int s) { return reinterpret_cast<long long*>(meta(s) + Cfg::META_TILE); };
   auto s_cnt = [&](int s) { return reinterpret_cast<unsigned*>(meta(s) + Cfg::META_CNT); };
-  auto s_map = [&](int s) { return reinterpret_cast<const uint32_t*>(smem + Cfg::OFF_MAP + size_t(s) * Cfg::MAP_BYTES); };
+  auto s_map = [&](int s) { return reinterpret_cast<const uint32_t*>(smem + Cfg::OFF_MAP + size_t(s) * Cfg::MAP_STRIDE); };
   auto s_rows = [&](int s) { return reinterpret_cast<acc_t*>(meta(s) + Cfg::META_ROWS); };
 
   const Pol pol{};
@@ -223,13 +227,18 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
           const uint64_t valid = (n - base < uint64_t(TILE)) ? (n - base) : uint64_t(TILE);
           const uint32_t bytes = uint32_t(valid * sizeof(in_t)) & ~15u;
           uint32_t map_bytes = 0;
-          if constexpr (Heads::kBitmap) map_bytes = uint32_t((valid + 127) / 128) * 16u;
+          if constexpr (Heads::kBitmap) {
+            map_bytes = uint32_t((valid + 127) / 128) * 16u;
+            // reductions: a full tile that is not the array's last brings the
+            // next tile's first head bits along (the bitmap is padded past n)
+            if (REDUCE && valid == uint64_t(TILE) && base + TILE < n) map_bytes += 16u;
+          }
           if (bytes + map_bytes) {
             ptx::mbar_arrive_expect_tx(&full[s], bytes + map_bytes);
             if (bytes)
               ptx::bulk_g2s(smem + size_t(s) * Cfg::TILE_BYTES, in + base * sizeof(in_t), bytes, &full[s], pol_l2);
             if (map_bytes)
-              ptx::bulk_g2s(smem + Cfg::OFF_MAP + size_t(s) * Cfg::MAP_BYTES,
+              ptx::bulk_g2s(smem + Cfg::OFF_MAP + size_t(s) * Cfg::MAP_STRIDE,
                             reinterpret_cast<const unsigned char*>(sargs.heads) + base / 8, map_bytes, &full[s],
                             pol_l2);
             pending |= 1u << s;
@@ -408,7 +417,8 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
       return hb;
     };
     // reduce: bit j set when element e0 + j ends its segment (the next
-    // element is a head, or e0 + j is the array's last element)
+    // element is a head, or e0 + j is the array's last element). The head bit
+    // of the element after a full tile is in the stage's map slot too.
     auto end_bits = [&](int s, int e0, uint64_t base, int valid) -> uint32_t {
       if (e0 + V < valid) {
         // e0 is a multiple of V and V divides 32: bits e0 .. e0+V-1 share a word
@@ -422,13 +432,9 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
         const int e = e0 + j;
         if (e < valid) {
           const uint64_t g = base + uint64_t(e) + 1;
-          uint32_t b;
-          if (g >= n)
-            b = 1u;
-          else if (e + 1 < valid)
-            b = (s_map(s)[(e + 1) >> 5] >> ((e + 1) & 31)) & 1u;
-          else
-            b = (__ldg(sargs.heads + (g >> 5)) >> (g & 31)) & 1u;  // first element of the next tile
+          // g < n: element e + 1 is in this tile, or it starts the next one
+          // (this tile is full and not the last)
+          const uint32_t b = g >= n ? 1u : (s_map(s)[(e + 1) >> 5] >> ((e + 1) & 31)) & 1u;
           en |= b << j;
         }
       }
@@ -691,10 +697,10 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
               end = true;  // the last element of the array ends its segment
             } else if (j + 1 < V) {
               end = (hb >> (j + 1)) & 1u;
-            } else if (e1 < valid) {
-              end = (s_map(s)[e1 >> 5] >> (e1 & 31)) & 1u;
             } else {
-              end = (__ldg(sargs.heads + ((base + uint64_t(e1)) >> 5)) >> ((base + e1) & 31)) & 1u;
+              // in this tile, or the first element of the next (this tile is
+              // full and not the last: its map slot holds that head bit)
+              end = (s_map(s)[e1 >> 5] >> (e1 & 31)) & 1u;
             }
             if (end) {
               const acc_t v = pol.aop(pc, a[j]);

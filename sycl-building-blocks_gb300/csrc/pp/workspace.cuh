@@ -57,6 +57,14 @@ struct WsHeader {
   unsigned int bar_gen;               // grid barrier generation
   unsigned int debug_spin;            // unused padding / diagnostics
   unsigned int pad_;
+  // look-back counters, kept only while the descriptor perturbation knob is
+  // on (ScanArgs::debug_delay_ns != 0) and never re-armed by a launch:
+  // [0] tiles whose nearest predecessor already held its inclusive prefix
+  //     (reduce-then-scan), [1] tiles that folded published aggregates back to
+  //     an older prefix (scan-then-reduce), [2] look-backs that folded more
+  //     than 32 predecessors (two or more windows), [3] polls that met a
+  //     descriptor whose words carried different tags (half written)
+  unsigned long long dbg[4];
 };
 
 constexpr size_t kHeaderBytes = 4096;
@@ -84,6 +92,38 @@ struct desc_codec {
     for (int i = 0; i < W; ++i) {
       const uint32_t w = i < PW ? p.w[i < PW ? i : 0] : 0u;
       atomicMax(reinterpret_cast<unsigned long long*>(d + i), (unsigned long long)(hi | w));
+    }
+  }
+
+  // publish() with `gap_ns` between the words of a multi-word descriptor, so
+  // that readers can meet it half written (descriptor perturbation knob).
+  __device__ __forceinline__ static void publish_spaced(uint64_t* d, const C& v, uint32_t tag, uint32_t gap_ns) {
+    words<C> p = to_words(v);
+    const uint64_t hi = uint64_t(tag) << 32;
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      if (i > 0 && gap_ns) ptx::nanosleep(gap_ns);
+      const uint32_t w = i < PW ? p.w[i < PW ? i : 0] : 0u;
+      atomicMax(reinterpret_cast<unsigned long long*>(d + i), (unsigned long long)(hi | w));
+    }
+  }
+
+  // True when the words of a loaded descriptor carry different tags and one
+  // of them is of epoch tag `etag`: a descriptor caught between the atomic
+  // updates of its words (decode() rejects it).
+  __device__ __forceinline__ static bool torn(const uint64_t (&w)[W], uint32_t etag) {
+    if constexpr (W == 1) {
+      return false;
+    } else {
+      const uint32_t t0 = uint32_t(w[0] >> 32);
+      bool differ = false, current = (t0 >> 2) == etag;
+#pragma unroll
+      for (int i = 1; i < W; ++i) {
+        const uint32_t ti = uint32_t(w[i] >> 32);
+        differ |= ti != t0;
+        current |= (ti >> 2) == etag;
+      }
+      return differ && current;
     }
   }
 

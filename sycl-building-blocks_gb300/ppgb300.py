@@ -48,6 +48,7 @@ EXPORTS = [
     "pp_decoupled_scan_host", "pp_cooperative_scan_host", "pp_scan_host", "pp_reduce_host", "pp_status_string",
     "pp_stream_status", "pp_workspace_status", "pp_set_timeout_ns", "pp_set_max_ctas", "pp_debug_set_skip_tile",
     "pp_version", "pp_decoupled_scan_device_noalloc", "pp_segmented_scan", "pp_segmented_reduce", "pp_rows_scan",
+    "pp_debug_set_lookback_delay", "pp_debug_lookback_counters",
 ]
 
 
@@ -91,6 +92,8 @@ def lib() -> C.CDLL:
     L.pp_set_timeout_ns.argtypes = [u64]
     L.pp_set_max_ctas.argtypes = [i32]
     L.pp_debug_set_skip_tile.argtypes = [C.c_longlong]
+    L.pp_debug_set_lookback_delay.argtypes = [C.c_uint32, C.c_uint32]
+    L.pp_debug_lookback_counters.argtypes = [vp, C.POINTER(C.c_uint64)]
     L.pp_version.restype = C.c_char_p
     for name in EXPORTS:
         if name not in ("pp_status_string", "pp_version"):
@@ -269,6 +272,21 @@ def set_max_ctas(ctas: int) -> None:
 
 def debug_set_skip_tile(tile: int) -> None:
     _check(lib().pp_debug_set_skip_tile(tile), "pp_debug_set_skip_tile")
+
+
+def debug_set_lookback_delay(max_delay_ns: int, seed: int = 0) -> None:
+    """Descriptor perturbation for tests (0 = off): pseudo-random delays of up
+    to max_delay_ns before every descriptor publication of decoupled scans."""
+    _check(lib().pp_debug_set_lookback_delay(max_delay_ns, seed), "pp_debug_set_lookback_delay")
+
+
+def debug_lookback_counters(stream: int = 0) -> dict:
+    """Read and clear the look-back counters gathered while the perturbation
+    was on (synchronises `stream`)."""
+    c = (C.c_uint64 * 4)()
+    _check(lib().pp_debug_lookback_counters(stream, c), "pp_debug_lookback_counters")
+    return {"reduce_then_scan": int(c[0]), "scan_then_reduce": int(c[1]), "over_32_predecessors": int(c[2]),
+            "half_written_reads": int(c[3])}
 
 
 def version() -> str:

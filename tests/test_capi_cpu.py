@@ -38,6 +38,10 @@ def test_host_side_argument_checks(pp):
     assert L.pp_scan(None, 0, 0, 1, None, dummy, 10, 0, 0) == pp.PP_ERR_INVALID_ARG
     assert L.pp_scan(None, 0, 2, 4, dummy, dummy, 10, 0, 0) == pp.PP_ERR_UNSUPPORTED  # bit_and on f32
     assert L.pp_scan(None, 0, 0, 1, dummy, dummy, 10, 0, 1) == pp.PP_ERR_UNSUPPORTED  # compensated u32
+    # the descriptor perturbation knob: bounded delays only, a counters buffer required
+    assert L.pp_debug_set_lookback_delay(2_000_000, 0) == pp.PP_ERR_INVALID_ARG
+    assert L.pp_debug_set_lookback_delay(0, 0) == pp.PP_OK
+    assert L.pp_debug_lookback_counters(None, None) == pp.PP_ERR_INVALID_ARG
     assert L.pp_scan(None, 0, 1, 4, dummy, dummy, 10, 0, 2) == pp.PP_ERR_UNSUPPORTED  # fp64-carry multiplies
     assert L.pp_scan(None, 0, 0, 1, dummy, dummy, 0, 0, 0) == pp.PP_OK  # n == 0 is a no-op
     assert L.pp_scan_ws(None, 0, 0, 1, dummy, dummy, 10, 0, 0, None, 0) == pp.PP_ERR_INVALID_ARG
