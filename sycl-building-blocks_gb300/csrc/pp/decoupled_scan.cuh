@@ -870,8 +870,11 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
       // into it is an async-proxy write
       ptx::fence_proxy_async_smem();
     };
-    // aggregate of segment seg of stage s (a warp-wide value)
-    auto reduce_segment = [&](int s, int seg, const StagedGeom& g) -> acc_t {
+    // aggregate of segment seg of stage s (a warp-wide value); rows layout:
+    // `info` gets the policy's statistic of this lane's row (fast rows)
+    using RF = row_fast_traits<Pol>;
+    using row_info_t = typename RF::info_t;
+    auto reduce_segment = [&](int s, int seg, const StagedGeom& g, row_info_t& info) -> acc_t {
       acc_t r = pol.aid();
       if constexpr (LAY == 2) {
         // this lane's row, in order; the scan of the row totals over the
@@ -879,13 +882,18 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
         // row's exclusive prefix stays for the scan pass
         const int r0 = seg * Cfg::SEG + lane * (CH * V);
         const bool interior = g.lo == 0 && g.blo == 0 && g.bhi == TILE;
+        row_info_t m = RF::id(pol);
 #pragma unroll
         for (int c = 0; c < CH; ++c) {
           in_t x[V];
           load_raw_at(s, r0 + c * V, g, interior, x);
 #pragma unroll
-          for (int j = 0; j < V; ++j) r = pol.aop_in(r, x[j]);
+          for (int j = 0; j < V; ++j) {
+            r = pol.aop_in(r, x[j]);
+            if constexpr (RF::value) m = RF::add(pol, m, x[j]);
+          }
         }
+        info = m;
         const acc_t inc = warp_inclusive_scan(r, aop, lane);
         const acc_t ex = shfl_up(inc, 1);
         s_rows(s)[seg * 32 + lane] = lane == 0 ? pol.aid() : ex;
@@ -949,7 +957,7 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
     };
     // reduce pass of use k over the segments of this warp: returns false at
     // the end of work or on a failed wait
-    auto reduce_pass = [&](int k) -> bool {
+    auto reduce_pass = [&](int k, row_info_t& info) -> bool {
       const int s = k % STAGES;
       const unsigned long long tw = Trace::kOn ? ptx::globaltimer_ns() : 0ull;
       if (!mbar_wait_bounded(&full[s], (k / STAGES) & 1, hdr, tmo, 0ull)) return false;
@@ -960,16 +968,18 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
         trace_now(kTrRGot, tile);
       }
       const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(tile, n, head);
-      record_segment(s, w, tile, reduce_segment(s, w, g));
+      record_segment(s, w, tile, reduce_segment(s, w, g, info));
       if (lane == 0) ptx::mbar_arrive(&aggb[s]);
       __syncwarp();
       return true;
     };
 
-    // the reduce pass runs one tile ahead of the scan pass
-    bool have = reduce_pass(0);
+    // the reduce pass runs one tile ahead of the scan pass (row statistics:
+    // info_cur of tile k, info_next of tile k + 1)
+    row_info_t info_cur = RF::id(pol), info_next = RF::id(pol);
+    bool have = reduce_pass(0, info_cur);
     for (int k = 0; have; ++k) {
-      const bool have_next = reduce_pass(k + 1);
+      const bool have_next = reduce_pass(k + 1, info_next);
       const int s = k % STAGES;
       // scan pass of use k
       if constexpr (Trace::kOn)
@@ -990,8 +1000,9 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
         const bool interior = g.lo == 0 && g.blo == 0 && g.bhi == TILE;
         const acc_t ex = s_rows(s)[w * 32 + lane];
         typename Pol::row_t row = pol.row_start(pol.extend(pw, ex));
-        auto chain = [&](auto excl_c) {
+        auto chain = [&](auto excl_c, auto fast_c) {
           constexpr bool kEx = decltype(excl_c)::value;
+          constexpr bool kFast = decltype(fast_c)::value;
           union Out {
             uint4 u;
             out_t x[V];
@@ -1002,14 +1013,32 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
             load_raw_at(s, r0 + c * V, g, interior, x);
             Out o;
 #pragma unroll
-            for (int j = 0; j < V; ++j) o.x[j] = kEx ? pol.row_excl(row, x[j]) : pol.row_incl(row, x[j]);
+            for (int j = 0; j < V; ++j) {
+              if constexpr (kFast)
+                o.x[j] = kEx ? RF::excl(pol, row, x[j]) : RF::incl(pol, row, x[j]);
+              else
+                o.x[j] = kEx ? pol.row_excl(row, x[j]) : pol.row_incl(row, x[j]);
+            }
             *reinterpret_cast<uint4*>(stage + size_t(r0 + c * V) * sizeof(in_t)) = o.u;
           }
         };
-        if (excl_kind)
-          chain(std::true_type{});
-        else
-          chain(std::false_type{});
+        // fast rows when every lane's row qualifies (a warp-uniform choice)
+        bool fast = false;
+        if constexpr (RF::value) fast = __all_sync(kFullMask, RF::ok(pol, row, info_cur, CH * V));
+        if constexpr (RF::value) {
+          if (fast) {
+            if (excl_kind)
+              chain(std::true_type{}, std::true_type{});
+            else
+              chain(std::false_type{}, std::true_type{});
+          }
+        }
+        if (!fast) {
+          if (excl_kind)
+            chain(std::true_type{}, std::false_type{});
+          else
+            chain(std::false_type{}, std::false_type{});
+        }
         store_segment(stage, g);
       } else {
       acc_t X = pol.aid();
@@ -1058,6 +1087,7 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
         ptx::mbar_arrive(BS == 2 ? &scanned[s] : &empty[s]);
       }
       have = have_next;
+      info_cur = info_next;
     }
   }
   if constexpr (BS != 0) ptx::bulk_wait<0>();  // this thread's bulk stores are complete

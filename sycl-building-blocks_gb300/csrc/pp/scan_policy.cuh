@@ -16,6 +16,8 @@
 // chain in FP64.
 #pragma once
 
+#include <type_traits>
+
 #include <cuda_runtime.h>
 
 #include "ops.cuh"
@@ -149,6 +151,61 @@ struct CompensatedF32 {
     r = aop_in(r, x);
     return o;
   }
+  // Fast rows (scan pass): the reduce pass also records max |x| of each row.
+  // When the row's starting prefix satisfies |hi| >= (k + 3) * max|x| for a
+  // row of k elements, every running hi of the row stays at least max|x| in
+  // magnitude, so Dekker's FastTwoSum (3 operations) gives exactly the sum
+  // and error TwoSum (6) would: the outputs are the same bit for bit.
+  static constexpr bool kRowFast = true;
+  using row_info_t = float;
+  __device__ __forceinline__ row_info_t row_info_id() const { return 0.0f; }
+  __device__ __forceinline__ row_info_t row_info_add(row_info_t m, float x) const { return fmaxf(m, fabsf(x)); }
+  __device__ __forceinline__ bool row_fast_ok(const row_t& r, row_info_t m, int k) const {
+    return fabsf(r.hi) >= __fmul_rn(float(k + 3), m);
+  }
+  __device__ __forceinline__ out_t row_incl_fast(row_t& r, float x) const {
+    float s, e;
+    fast_two_sum(r.hi, x, s, e);
+    r = ff32{s, __fadd_rn(r.lo, e)};
+    return __fadd_rn(r.hi, r.lo);
+  }
+  __device__ __forceinline__ out_t row_excl_fast(row_t& r, float x) const {
+    const float o = __fadd_rn(r.hi, r.lo);
+    float s, e;
+    fast_two_sum(r.hi, x, s, e);
+    r = ff32{s, __fadd_rn(r.lo, e)};
+    return o;
+  }
+};
+
+// Policies without a fast row path (kRowFast absent) see these defaults.
+template <class Pol, class = void>
+struct row_fast_traits {
+  static constexpr bool value = false;
+  using info_t = int;
+  using row_t = typename Pol::row_t;
+  using in_t = typename Pol::in_t;
+  using out_t = typename Pol::out_t;
+  __device__ __forceinline__ static info_t id(const Pol&) { return 0; }
+  __device__ __forceinline__ static info_t add(const Pol&, info_t m, const in_t&) { return m; }
+  __device__ __forceinline__ static bool ok(const Pol&, const row_t&, info_t, int) { return false; }
+  __device__ __forceinline__ static out_t incl(const Pol& p, row_t& r, const in_t& x) { return p.row_incl(r, x); }
+  __device__ __forceinline__ static out_t excl(const Pol& p, row_t& r, const in_t& x) { return p.row_excl(r, x); }
+};
+template <class Pol>
+struct row_fast_traits<Pol, std::void_t<decltype(Pol::kRowFast)>> {
+  static constexpr bool value = Pol::kRowFast;
+  using info_t = typename Pol::row_info_t;
+  using row_t = typename Pol::row_t;
+  using in_t = typename Pol::in_t;
+  using out_t = typename Pol::out_t;
+  __device__ __forceinline__ static info_t id(const Pol& p) { return p.row_info_id(); }
+  __device__ __forceinline__ static info_t add(const Pol& p, info_t m, const in_t& x) { return p.row_info_add(m, x); }
+  __device__ __forceinline__ static bool ok(const Pol& p, const row_t& r, info_t m, int k) {
+    return p.row_fast_ok(r, m, k);
+  }
+  __device__ __forceinline__ static out_t incl(const Pol& p, row_t& r, const in_t& x) { return p.row_incl_fast(r, x); }
+  __device__ __forceinline__ static out_t excl(const Pol& p, row_t& r, const in_t& x) { return p.row_excl_fast(r, x); }
 };
 
 struct F64CarryF32 {
