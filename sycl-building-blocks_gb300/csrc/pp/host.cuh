@@ -517,7 +517,10 @@ using SegCfgOf = SegCfg<SegPlainScan<T, Op>, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW
 // nonempty flags, ranks, rank -> segment map.
 struct SegWsLayout {
   size_t control_bytes;
-  size_t bitmap_off, bitmap_bytes, nonempty_off, rank_off, rank_out_off, scratch_bytes;
+  size_t bitmap_off, bitmap_bytes, nonempty_off, rank_off, rank_out_off;
+  size_t tile_base_off, tile_rec_off, tile_rec_bytes;  // reduce: per-tile base ranks and records
+  size_t chunk_v_off, chunk_c_off;                     // reduce: per-chunk summaries of the records
+  size_t scratch_bytes;
 };
 template <class T, class Op>
 inline SegWsLayout seg_ws_layout(uint64_t n, uint64_t num_segments, bool csr, bool reduce) {
@@ -548,6 +551,16 @@ inline SegWsLayout seg_ws_layout(uint64_t n, uint64_t num_segments, bool csr, bo
   if (reduce) off += align_up(num_segments * 4, 256);
   L.rank_out_off = off;  // reduce: totals by rank
   if (reduce) off += align_up(num_segments * sizeof(T), 256);
+  L.tile_base_off = off;  // reduce: sized for the smallest tile of any variant
+  if (reduce) off += align_up(ntiles * 4, 256);
+  L.tile_rec_off = off;
+  L.tile_rec_bytes = reduce ? ntiles * sizeof(SegTileRec<T>) : 0;
+  off += align_up(L.tile_rec_bytes, 256);
+  const uint64_t nchunks = (ntiles + kSegChunk - 1) / kSegChunk;
+  L.chunk_v_off = off;
+  if (reduce) off += align_up(nchunks * sizeof(T), 256);
+  L.chunk_c_off = off;
+  if (reduce) off += align_up(nchunks * 4, 256);
   L.scratch_bytes = off;
   return L;
 }
@@ -559,8 +572,23 @@ inline Status acquire_scratch(cudaStream_t s, size_t need, unsigned char** out) 
   return st;
 }
 
+// What a CSR reduction adds to the main launch: per-tile base ranks before it
+// (from the offsets and the rank scan of the non-empty flags), the per-tile
+// records zero-filled, and the fix-up of segments that cross tiles after it.
+struct SegReduceExtra {
+  const int64_t* offsets = nullptr;
+  const uint32_t* nonempty = nullptr;
+  const uint32_t* rank = nullptr;
+  uint32_t* tile_base = nullptr;
+  void* tile_rec = nullptr;
+  size_t tile_rec_bytes = 0;
+  void* chunk_v = nullptr;
+  uint32_t* chunk_c = nullptr;
+};
+
 template <class Tn, class Pol, class Heads, bool REVERSE, bool REDUCE, bool SKIP = false>
-inline Status launch_segmented_variant(cudaStream_t s, const SegArgs& a) {
+inline Status launch_segmented_variant(cudaStream_t s, const SegArgs& a0, uint64_t num_segments = 0,
+                                       const SegReduceExtra* rx = nullptr) {
   constexpr int BS = REDUCE ? 0 : Tn::BS;  // the store warp serves scans only
   using Cfg = SegCfg<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Tn::VB, Tn::LAY, (BS == 2 ? 1 : 0)>;
   auto k = segmented_staged_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Heads, REVERSE, REDUCE, Tn::VB, Tn::LAY,
@@ -571,17 +599,44 @@ inline Status launch_segmented_variant(cudaStream_t s, const SegArgs& a) {
   int bps = 0;
   st = prepare_kernel(k, Cfg::THREADS, Cfg::SMEM, bps);
   if (st != Status::ok) return st;
-  const uint64_t ntiles = (a.s.n + Cfg::TILE - 1) / Cfg::TILE;
+  const uint64_t ntiles = (a0.s.n + Cfg::TILE - 1) / Cfg::TILE;
+  SegArgs a = a0;
+  if constexpr (REDUCE) {
+    if (!rx || rx->tile_rec_bytes < ntiles * sizeof(SegTileRec<typename Pol::in_t>)) return Status::workspace;
+    a.tile_base = rx->tile_base;
+    a.tile_rec = rx->tile_rec;
+    const unsigned tgrid = unsigned((ntiles + 7) / 8 < 4096 ? (ntiles + 7) / 8 : 4096);  // a warp per tile
+    segment_tile_base_kernel<<<tgrid, 256, 0, s>>>(rx->offsets, rx->nonempty, rx->rank, num_segments,
+                                                   uint64_t(Cfg::TILE), ntiles, rx->tile_base);
+    if (cudaGetLastError() != cudaSuccess) return Status::cuda;
+    if (cudaMemsetAsync(rx->tile_rec, 0, ntiles * sizeof(SegTileRec<typename Pol::in_t>), s) != cudaSuccess)
+      return Status::cuda;
+  }
   uint64_t grid = uint64_t(bps) * di.sm_count;
   const int cap = settings().max_ctas.load();
   if (cap > 0 && uint64_t(cap) < grid) grid = cap;
   if (ntiles < grid) grid = ntiles;
   k<<<unsigned(grid), Cfg::THREADS, Cfg::SMEM, s>>>(a);
-  return from_cuda(cudaGetLastError());
+  if (cudaGetLastError() != cudaSuccess) return Status::cuda;
+  if constexpr (REDUCE) {
+    using T = typename Pol::in_t;
+    using Op = decltype(Pol{}.op);
+    const auto* rec = static_cast<const SegTileRec<T>*>(rx->tile_rec);
+    const uint64_t nchunks = (ntiles + kSegChunk - 1) / kSegChunk;
+    segment_chunk_kernel<T, Op><<<unsigned(nchunks), 256, 0, s>>>(rec, ntiles, static_cast<T*>(rx->chunk_v),
+                                                                  rx->chunk_c);
+    if (cudaGetLastError() != cudaSuccess) return Status::cuda;
+    const unsigned fgrid = unsigned((ntiles + 7) / 8 < 4096 ? (ntiles + 7) / 8 : 4096);  // a warp per tile
+    segment_fixup_kernel<T, Op><<<fgrid, 256, 0, s>>>(rec, ntiles, static_cast<const T*>(rx->chunk_v), rx->chunk_c,
+                                                      rx->tile_base, static_cast<T*>(a.rank_out));
+    if (cudaGetLastError() != cudaSuccess) return Status::cuda;
+  }
+  return Status::ok;
 }
 
 template <class Pol, class Heads, bool REVERSE, bool REDUCE>
-inline Status launch_segmented(cudaStream_t s, const SegArgs& a, uint64_t num_segments = 0) {
+inline Status launch_segmented(cudaStream_t s, const SegArgs& a, uint64_t num_segments = 0,
+                               const SegReduceExtra* rx = nullptr) {
   using T = typename Pol::in_t;
   if constexpr (Heads::kBitmap && !REVERSE) {
     const bool long_segments = num_segments == 0 || a.s.n / num_segments >= kSegLongMean;
@@ -589,9 +644,11 @@ inline Status launch_segmented(cudaStream_t s, const SegArgs& a, uint64_t num_se
     // faster at mean lengths of 900-5,900; scans gain nothing from it, and
     // both lose 2-8 % with it at mean lengths below 100)
     if (long_segments)
-      return launch_segmented_variant<SegTunedCsr<T, true>, Pol, Heads, REVERSE, REDUCE, REDUCE>(s, a);
-    return launch_segmented_variant<SegTunedCsr<T, false>, Pol, Heads, REVERSE, REDUCE>(s, a);
+      return launch_segmented_variant<SegTunedCsr<T, true>, Pol, Heads, REVERSE, REDUCE, REDUCE>(s, a, num_segments,
+                                                                                                rx);
+    return launch_segmented_variant<SegTunedCsr<T, false>, Pol, Heads, REVERSE, REDUCE>(s, a, num_segments, rx);
   } else {
+    static_assert(!REDUCE, "reductions take CSR segments");
     return launch_segmented_variant<SegUniform<T>, Pol, Heads, REVERSE, REDUCE>(s, a);
   }
 }
@@ -668,7 +725,16 @@ inline Status segmented_reduce(cudaStream_t s, const T* in, uint64_t n, const in
   a.s.debug_skip_tile = -1;
   a.heads = heads;
   a.rank_out = by_rank;
-  st = launch_segmented<SegPlainScan<T, Op>, CsrHeads, false, true>(s, a, num_segments);
+  SegReduceExtra rx;
+  rx.offsets = offsets;
+  rx.nonempty = nonempty;
+  rx.rank = rank;
+  rx.tile_base = reinterpret_cast<uint32_t*>(base + L.tile_base_off);
+  rx.tile_rec = base + L.tile_rec_off;
+  rx.tile_rec_bytes = L.tile_rec_bytes;
+  rx.chunk_v = base + L.chunk_v_off;
+  rx.chunk_c = reinterpret_cast<uint32_t*>(base + L.chunk_c_off);
+  st = launch_segmented<SegPlainScan<T, Op>, CsrHeads, false, true>(s, a, num_segments, &rx);
   if (st != Status::ok) return st;
   segment_gather_kernel<T><<<pre_grid, 256, 0, s>>>(nonempty, rank, by_rank, num_segments, out);
   return from_cuda(cudaGetLastError());

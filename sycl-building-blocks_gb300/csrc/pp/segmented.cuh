@@ -22,14 +22,21 @@
 // the last to the first and mirror the element order inside each tile; they
 // are provided for uniform segments.
 //
-// Segmented reduce writes no scanned array: the element that ends a
-// non-empty segment writes the segment's value to rank_out[count - 1] (its
-// rank among the non-empty segments: a store with no load in front of it),
-// and segment_gather_kernel moves the totals to their segments; empty
-// segments get the identity from the pre-pass. In the rows layout it reads
-// the data once: the reduce pass leaves each row's running value at the
-// row's segment ends and keeps the row's head and end bits, and once the
-// tile's prefix is known only the end elements are read again.
+// Segmented reduce writes no scanned array and needs no look-back: every
+// tile reduces on its own, with tile-local prefixes only. The element that
+// ends a non-empty segment whose head lies in the same tile writes the
+// segment's total to rank_out[base + count - 1] (base: the non-empty segments
+// that start before the tile, from a binary search over the offsets; count:
+// the heads of the tile up to the element), a store with no load in front of
+// it. The one segment per tile that was open where the tile begins and ends
+// inside it leaves its piece in the tile's record, beside the tile's
+// aggregate; segment_fixup_kernel scans the records in tile order and
+// completes those segments, and segment_gather_kernel moves the totals from
+// rank order to their segments (empty segments get the identity from the
+// pre-pass). In the rows layout the data is read once: the reduce pass
+// leaves each row's running value at the row's segment ends and keeps the
+// row's head and end bits, and the totals pass reads only the end elements.
+// A stage is free as soon as its tile's totals are written.
 #pragma once
 
 #include <cstdint>
@@ -81,6 +88,20 @@ struct SegArgs {
   const uint32_t* heads;         // CSR: n-bit head bitmap (tile-padded), else null
   uint64_t seg_len;              // uniform: row length
   void* rank_out;                // reduce: total of each non-empty segment, by rank
+  const uint32_t* tile_base;     // reduce: non-empty segments that start before each tile
+  void* tile_rec;                // reduce: SegTileRec<T> per tile (zero-filled before the launch)
+};
+
+// Per-tile record of a segmented reduce: the tile's aggregate pair and the
+// piece of the segment that was open where the tile begins and ends inside
+// it (its value from the tile's start to its end; flag 1 when there is one).
+// segment_fixup_kernel completes those segments in tile order.
+template <class T>
+struct SegTileRec {
+  T agg_v;
+  uint32_t agg_c;
+  T piece_v;
+  uint32_t piece_flag;
 };
 
 // NC compute warps, CH chunks per lane, VB bytes per chunk (the vector width
@@ -257,7 +278,8 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
     __syncwarp();
   } else if (warp == 1) {
     // ------------------------------------------------------------ look-back
-    for (int k = 0;; ++k) {
+    // (a reduction needs none: its tiles are independent)
+    for (int k = 0; !REDUCE; ++k) {
       const int s = k % STAGES;
       const uint32_t par = (k / STAGES) & 1;
       if (!mbar_wait_bounded(&full[s], par, hdr, tmo, 0ull)) break;
@@ -393,8 +415,8 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
       bulk = int((uint32_t(valid * sizeof(in_t)) & ~15u) / sizeof(in_t));
       mt = Heads::kBitmap ? 0 : base % seg_len;
     };
-    // rows (LAY 2): V raw elements at tile offset e0 with their head bits
-    auto load_row_chunk = [&](int s, int e0, uint64_t base, int valid, int bulk, in_t (&x)[V]) -> uint32_t {
+    // rows (LAY 2): V raw elements at tile offset e0 (no head bits)
+    auto load_row_vals = [&](int s, int e0, uint64_t base, int valid, int bulk, in_t (&x)[V]) {
       const unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
       if (e0 + V <= bulk) {
         union {
@@ -412,33 +434,33 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
                           : (p < valid ? gin[base + p] : identity<decltype(pol.op), in_t>());
         }
       }
-      uint32_t hb = (s_map(s)[e0 >> 5] >> (e0 & 31)) & ((1u << V) - 1u);
-      if (e0 + V > valid) hb &= (e0 >= valid) ? 0u : ((1u << (valid - e0)) - 1u);
-      return hb;
     };
-    // reduce: bit j set when element e0 + j ends its segment (the next
-    // element is a head, or e0 + j is the array's last element). The head bit
-    // of the element after a full tile is in the stage's map slot too.
-    auto end_bits = [&](int s, int e0, uint64_t base, int valid) -> uint32_t {
-      if (e0 + V < valid) {
-        // e0 is a multiple of V and V divides 32: bits e0 .. e0+V-1 share a word
-        const uint32_t here = s_map(s)[e0 >> 5] >> (e0 & 31);
-        const uint32_t next = (s_map(s)[(e0 + V) >> 5] >> ((e0 + V) & 31)) & 1u;
-        return ((here >> 1) & ((1u << (V - 1)) - 1u)) | (next << (V - 1));
+    // rows (LAY 2): head bits of the lane row starting at tile offset r0
+    // (bit i for element r0 + i, i < CH * V <= 32) from one 64-bit window of
+    // the stage's map, and in `ends` the elements that end their segment: the
+    // next element is a head, or the element is the array's last. The element
+    // after a full tile that is not the array's last is the next tile's first,
+    // whose head bit the map slot holds for reductions.
+    auto row_bits = [&](int s, int r0, uint64_t base, int valid, uint32_t& ends) -> uint32_t {
+      constexpr int CNT = CH * V;
+      auto low = [](int k) -> uint32_t { return k >= 32 ? 0xFFFFFFFFu : ((1u << k) - 1u); };
+      const uint32_t w0 = uint32_t(r0) >> 5;
+      const uint64_t win = ((uint64_t(s_map(s)[w0 + 1]) << 32) | s_map(s)[w0]) >> (r0 & 31);
+      const int nv = valid - r0;  // valid elements of this row
+      if (nv >= CNT) {
+        const uint32_t h = uint32_t(win) & low(CNT);
+        const uint32_t next =
+            (nv == CNT && base + uint64_t(valid) >= n) ? 1u : uint32_t(win >> CNT) & 1u;
+        ends = (h >> 1) | (next << (CNT - 1));
+        return h;
       }
-      uint32_t en = 0;
-#pragma unroll
-      for (int j = 0; j < V; ++j) {
-        const int e = e0 + j;
-        if (e < valid) {
-          const uint64_t g = base + uint64_t(e) + 1;
-          // g < n: element e + 1 is in this tile, or it starts the next one
-          // (this tile is full and not the last)
-          const uint32_t b = g >= n ? 1u : (s_map(s)[(e + 1) >> 5] >> ((e + 1) & 31)) & 1u;
-          en |= b << j;
-        }
+      if (nv > 0) {  // the array's last tile: its last element ends its segment
+        const uint32_t h = uint32_t(win) & low(nv);
+        ends = ((h >> 1) & low(nv - 1)) | (1u << (nv - 1));
+        return h;
       }
-      return en;
+      ends = 0u;
+      return 0u;
     };
     // reduce: head and end bits of this lane's row in the tile of the last
     // reduce pass (bit c * V + j for element j of chunk c)
@@ -468,15 +490,15 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
           // not read again but for those), and the row's head and end bits
           // are kept for the totals
           unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
-          uint32_t hpk = 0, epk = 0;
+          uint32_t epk = 0;
+          const uint32_t hpk = row_bits(s, r0, base, valid, epk);
 #pragma unroll
           for (int c = 0; c < CH; ++c) {
             const int e0 = r0 + c * V;
             in_t x[V];
-            const uint32_t hb = load_row_chunk(s, e0, base, valid, bulk, x);
-            const uint32_t en = end_bits(s, e0, base, valid);
-            hpk |= hb << (c * V);
-            epk |= en << (c * V);
+            load_row_vals(s, e0, base, valid, bulk, x);
+            const uint32_t hb = (hpk >> (c * V)) & ((1u << V) - 1u);
+            const uint32_t en = (epk >> (c * V)) & ((1u << V) - 1u);
             if (!SKIP || __any_sync(kFullMask, (hb | en) != 0u)) {
               union {
                 vec_t u;
@@ -498,10 +520,13 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
           row_heads = hpk;
           row_ends = epk;
         } else {
+          uint32_t unused_ends;
+          const uint32_t hrow = row_bits(s, r0, base, valid, unused_ends);
 #pragma unroll
           for (int c = 0; c < CH; ++c) {
             in_t x[V];
-            const uint32_t hb = load_row_chunk(s, r0 + c * V, base, valid, bulk, x);
+            load_row_vals(s, r0 + c * V, base, valid, bulk, x);
+            const uint32_t hb = (hrow >> (c * V)) & ((1u << V) - 1u);
 #pragma unroll
             for (int j = 0; j < V; ++j) r = pol.aop(r, pol.load(x[j], (hb >> j) & 1u));
           }
@@ -537,20 +562,32 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
         if (lane == 0) {
           *s_tagg(s) = agg;
           *s_cnt(s) = 0u;
-          codec::publish(args.desc + tile * codec::W, agg, make_tag(etag, tile == 0 ? kPrefix : kAggregate));
-          trace_now(kTrAggPub, tile);
+          if constexpr (REDUCE) {
+            // no look-back: the totals pass works from the tile's start
+            SegTileRec<out_t>* rec = static_cast<SegTileRec<out_t>*>(sargs.tile_rec) + tile;
+            rec->agg_v = agg.v;
+            rec->agg_c = agg.c;
+            *s_pref(s) = pol.cid();
+            trace_now(kTrAggPub, tile);
+            ptx::mbar_arrive(&prefb[s]);
+          } else {
+            codec::publish(args.desc + tile * codec::W, agg, make_tag(etag, tile == 0 ? kPrefix : kAggregate));
+            trace_now(kTrAggPub, tile);
+          }
         }
       }
       __syncwarp();
-      if (lane == 0) ptx::mbar_arrive(&aggb[s]);
+      if (!REDUCE && lane == 0) ptx::mbar_arrive(&aggb[s]);
       __syncwarp();
       return true;
     };
 
+    // scans: the reduce pass runs one tile ahead of the scan pass; reductions
+    // finish each tile (totals from tile-local prefixes) before the next
     bool have = reduce_pass(0);
     for (int k = 0; have; ++k) {
       const uint32_t cur_heads = row_heads, cur_ends = row_ends;  // tile k
-      const bool have_next = reduce_pass(k + 1);
+      const bool have_next = REDUCE ? true : reduce_pass(k + 1);
       const int s = k % STAGES;
       if constexpr (Trace::kOn)
         if (w == 0 && lane == 0) trace_now(kTrPWait, *s_tile(s));
@@ -571,23 +608,34 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
           // values the reduce pass left at their last elements; the segment
           // that is open where the row begins (no head in the row up to its
           // end) adds the row's prefix
+          const uint32_t tbase = cur_ends ? __ldg(sargs.tile_base + tile) : 0u;
           for (uint32_t m = cur_ends; m != 0u; m &= m - 1u) {
             const int i = __ffs(m) - 1;
             const uint32_t h = __popc(cur_heads & (0xFFFFFFFFu >> (31 - i)));  // heads up to element i
             acc_t t = pol.load(reinterpret_cast<const out_t*>(stage)[r0 + i], false);
             if (h == 0) t = pol.aop(p, t);
-            const uint32_t cnt = p.c + h;  // rank + 1 of the segment
-            if (cnt > 0) static_cast<out_t*>(sargs.rank_out)[cnt - 1] = t.v;
+            const uint32_t cnt = p.c + h;  // heads of the tile up to element i
+            if (cnt > 0) {
+              static_cast<out_t*>(sargs.rank_out)[tbase + cnt - 1] = t.v;
+            } else {
+              // the segment open where the tile begins ends here
+              SegTileRec<out_t>* rec = static_cast<SegTileRec<out_t>*>(sargs.tile_rec) + tile;
+              rec->piece_v = t.v;
+              rec->piece_flag = 1u;
+            }
           }
           // the stage was written through the generic proxy; the producer's
           // next bulk copy into it is an async-proxy write
           ptx::fence_proxy_async_smem();
         } else {
           // a thread-serial chain per row
+          uint32_t unused_ends;
+          const uint32_t hrow = row_bits(s, r0, base, valid, unused_ends);
 #pragma unroll
           for (int c = 0; c < CH; ++c) {
             in_t x[V];
-            const uint32_t hb = load_row_chunk(s, r0 + c * V, base, valid, bulk, x);
+            load_row_vals(s, r0 + c * V, base, valid, bulk, x);
+            const uint32_t hb = (hrow >> (c * V)) & ((1u << V) - 1u);
             const int e0 = r0 + c * V;
             union {
               vec_t u;
@@ -703,8 +751,14 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
               end = (s_map(s)[e1 >> 5] >> (e1 & 31)) & 1u;
             }
             if (end) {
-              const acc_t v = pol.aop(pc, a[j]);
-              if (v.c > 0) static_cast<out_t*>(sargs.rank_out)[v.c - 1] = v.v;
+              const acc_t v = pol.aop(pc, a[j]);  // tile-local
+              if (v.c > 0) {
+                static_cast<out_t*>(sargs.rank_out)[__ldg(sargs.tile_base + tile) + v.c - 1] = v.v;
+              } else {
+                SegTileRec<out_t>* rec = static_cast<SegTileRec<out_t>*>(sargs.tile_rec) + tile;
+                rec->piece_v = v.v;
+                rec->piece_flag = 1u;
+              }
             }
           }
         }
@@ -715,7 +769,7 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
         if (w == 0) trace_now(kTrSDone, tile);
         ptx::mbar_arrive(BS == 2 ? &scanned[s] : &empty[s]);
       }
-      have = have_next;
+      have = REDUCE ? reduce_pass(k + 1) : have_next;
     }
   }
   if constexpr (BS == 2) ptx::bulk_wait<0>();  // this thread's bulk stores are complete
@@ -741,6 +795,121 @@ __global__ void segment_heads_kernel(const int64_t* offsets, uint64_t num_segmen
     if (nonempty) nonempty[s] = ne ? 1u : 0u;
     if (ne) atomicOr(heads + (uint64_t(b) >> 5), 1u << (uint64_t(b) & 31));
     if (reduce_out && !ne) reduce_out[s] = identity<Op, T>();
+  }
+}
+
+// Segmented reduce, before the main kernel: base[t] = the non-empty segments
+// that start before tile t (t * tile): one warp per tile finds the first
+// segment with offsets[s] >= t * tile by a 32-way search (about four dependent
+// loads for 2^16 segments, instead of sixteen for a binary search) and reads
+// the exclusive scan of the non-empty flags (`rank`) there. (A template only so
+// that every translation unit including this header may instantiate it.)
+template <class Index = int64_t>
+__global__ void segment_tile_base_kernel(const Index* offsets, const uint32_t* nonempty, const uint32_t* rank,
+                                         uint64_t num_segments, uint64_t tile, uint64_t ntiles, uint32_t* base) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t warps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t t = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5; t < ntiles; t += warps) {
+    const Index target = Index(t * tile);
+    uint64_t lo = 0, hi = num_segments;  // answer in [lo, hi]
+    while (hi - lo > 32) {
+      const uint64_t step = (hi - lo + 31) / 32;
+      const uint64_t probe = lo + uint64_t(lane) * step;  // offsets[probe] < target for the lanes below the answer
+      const bool below = probe < hi && offsets[probe] < target;
+      const uint32_t m = __ballot_sync(kFullMask, below);
+      const int k = __popc(m);  // lanes 0 .. k-1 are below
+      const uint64_t nlo = k == 0 ? lo : lo + uint64_t(k - 1) * step + 1;
+      const uint64_t nhi = lo + uint64_t(k) * step < hi ? lo + uint64_t(k) * step : hi;
+      lo = nlo;
+      hi = nhi;
+    }
+    const uint64_t probe = lo + uint64_t(lane);
+    const bool below = probe < hi && offsets[probe] < target;
+    const uint64_t first = lo + uint64_t(__popc(__ballot_sync(kFullMask, below)));
+    if (lane == 0) base[t] = first < num_segments ? rank[first] : rank[num_segments - 1] + nonempty[num_segments - 1];
+  }
+}
+
+// Segmented reduce, after the main kernel: per chunk of kSegChunk tiles, the
+// heads it holds and the reduction of its tiles' aggregates (used by the
+// fix-up to step over long head-free runs of tiles in one go).
+constexpr int kSegChunk = 1024;
+template <class T, class Op>
+__global__ void __launch_bounds__(256) segment_chunk_kernel(const SegTileRec<T>* rec, uint64_t ntiles, T* chunk_v,
+                                                            uint32_t* chunk_c) {
+  const Op op{};
+  __shared__ T s_v[8];
+  __shared__ uint32_t s_c[8];
+  const uint64_t b = uint64_t(blockIdx.x) * kSegChunk;
+  T v = identity<Op, T>();
+  uint32_t c = 0;
+  for (uint64_t t = b + threadIdx.x; t < b + kSegChunk && t < ntiles; t += 256) {
+    v = op(v, rec[t].agg_v);
+    c += rec[t].agg_c;
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_reduce(v, op, lane);
+  c = warp_reduce(c, plus{}, lane);
+  if (lane == 0) {
+    s_v[w] = v;
+    s_c[w] = c;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < 8; ++i) {
+      v = op(v, s_v[i]);
+      c += s_c[i];
+    }
+    chunk_v[blockIdx.x] = v;
+    chunk_c[blockIdx.x] = c;
+  }
+}
+
+// Segmented reduce, last: every tile whose record holds a piece (the segment
+// open where the tile begins ends inside it) gets the rest of that segment by
+// a warp-wide look-back over the earlier tiles' records: 32 tiles per step
+// back to the nearest tile with a head, whose aggregate is the segment's value
+// from its head; runs of kSegChunk head-free tiles are stepped over with their
+// chunk's reduction. The total goes to rank tile_base[t] - 1. Deterministic.
+template <class T, class Op>
+__global__ void __launch_bounds__(256) segment_fixup_kernel(const SegTileRec<T>* rec, uint64_t ntiles,
+                                                            const T* chunk_v, const uint32_t* chunk_c,
+                                                            const uint32_t* tile_base, T* rank_out) {
+  const Op op{};
+  const int lane = threadIdx.x & 31;
+  const uint64_t warps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t t = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5; t < ntiles; t += warps) {
+    if (!rec[t].piece_flag) continue;  // warp-uniform
+    T acc = rec[t].piece_v;            // the piece, then earlier tiles folded in front of it
+    long long hi = (long long)t;       // tiles [0, hi) remain
+    bool done = false;
+    while (!done && hi > 0) {
+      if (hi % kSegChunk == 0) {
+        const long long ch = hi / kSegChunk - 1;
+        if (chunk_c[ch] == 0) {  // a whole head-free chunk
+          acc = op(chunk_v[ch], acc);
+          hi -= kSegChunk;
+          continue;
+        }
+      }
+      const long long u = hi - 1 - lane;  // lane i reads tile hi - 1 - i
+      const bool ok = u >= 0 && u >= (hi - 1) / kSegChunk * kSegChunk;  // within this chunk
+      T v = identity<Op, T>();
+      uint32_t c = 0;
+      if (ok) {
+        v = rec[u].agg_v;
+        c = rec[u].agg_c;
+      }
+      const uint32_t hm = __ballot_sync(kFullMask, ok && c > 0);
+      const uint32_t okm = __ballot_sync(kFullMask, ok);
+      const int last = hm ? __ffs(hm) - 1 : 31 - __clz(okm);  // nearest head, else the chunk's first tile
+      if (lane > last) v = identity<Op, T>();
+      v = warp_reduce_reversed(v, [&](const T& x, const T& y) { return op(x, y); }, lane);  // lanes last .. 0
+      acc = op(v, acc);
+      if (hm) done = true;
+      hi -= last + 1;
+    }
+    if (lane == 0 && tile_base[t] > 0) rank_out[tile_base[t] - 1] = acc;
   }
 }
 

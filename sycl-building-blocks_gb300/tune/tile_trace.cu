@@ -14,7 +14,6 @@
 // configuration) on log-uniform segment lengths in [1, 2^16] that fill the
 // input; there the ticket slot holds when the producer began to wait for a
 // free stage (tickets are drawn once a stage is free).
-#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -190,6 +189,30 @@ int trace_seg(const char* name, int log2_bytes, const char* path) {
   CHECK(cudaMalloc(&fl, size_t(1) << 28));
   CHECK(cudaMemset(fl, 1, size_t(1) << 28));
   CHECK(cudaMalloc(&sink, 4));
+  // reductions: the non-empty segments before each tile (every segment here
+  // is non-empty, so that is the index of the first segment starting at or
+  // after the tile) and the per-tile records
+  uint32_t* tile_base = nullptr;
+  void* tile_rec = nullptr;
+  if (REDUCE) {
+    std::vector<uint32_t> tb(static_cast<size_t>(ntiles));
+    for (long long t = 0; t < ntiles; ++t) {
+      const int64_t target = int64_t(t) * Cfg::TILE;
+      size_t lo = 0, hi = S;  // first segment starting at or after the tile
+      while (lo < hi) {
+        const size_t mid = (lo + hi) / 2;
+        if (off[mid] < target)
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+      tb[size_t(t)] = uint32_t(lo);
+    }
+    CHECK(cudaMalloc(&tile_base, tb.size() * 4));
+    CHECK(cudaMemcpy(tile_base, tb.data(), tb.size() * 4, cudaMemcpyHostToDevice));
+    CHECK(cudaMalloc(&tile_rec, size_t(ntiles) * sizeof(SegTileRec<T>)));
+    CHECK(cudaMemset(tile_rec, 0, size_t(ntiles) * sizeof(SegTileRec<T>)));
+  }
   SegArgs a{};
   a.s.in = in;
   a.s.out = REDUCE ? nullptr : out;
@@ -200,6 +223,8 @@ int trace_seg(const char* name, int log2_bytes, const char* path) {
   a.s.debug_skip_tile = -1;
   a.heads = heads;
   a.rank_out = REDUCE ? out : nullptr;
+  a.tile_base = tile_base;
+  a.tile_rec = tile_rec;
   for (int i = 0; i < 3; ++i) k<<<grid, Cfg::THREADS, Cfg::SMEM>>>(a);
   const long long nrec = ntiles < kMaxTiles ? ntiles : kMaxTiles;
   unsigned long long* tr = nullptr;
@@ -237,6 +262,8 @@ int trace_seg(const char* name, int log2_bytes, const char* path) {
   cudaFree(ws);
   cudaFree(heads);
   cudaFree(d_off);
+  if (tile_base) cudaFree(tile_base);
+  if (tile_rec) cudaFree(tile_rec);
   cudaFree(in);
   cudaFree(out);
   return err == 0 ? 0 : 3;

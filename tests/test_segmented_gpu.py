@@ -142,6 +142,17 @@ def _reduce_and_check(pp, oracle, cuda, dtype, op, lens):
             assert got[k] == oracle.reduce(seg, op), (k, seg.size, got[k], oracle.reduce(seg, op))
 
 
+@pytest.mark.parametrize("dtype", ["i32", "f32", "i64", "f64"])
+@pytest.mark.parametrize("op", ["plus", "maximum"])
+@pytest.mark.parametrize("lens", [[40_000_003, 0, 7, 17_000_000, 1, 0], [16_515_072, 33_030_144, 5]])
+def test_segmented_reduce_segments_across_chunks(pp, oracle, cuda, dtype, op, lens):
+    """Segments spanning thousands of tiles: the reduction's fix-up steps over
+    whole head-free chunks of 1,024 tile records. The second case puts its
+    heads exactly on chunk boundaries (16,515,072 = 1,024 tiles of 16,128
+    4-byte elements = 2,048 tiles of 8,064 8-byte elements)."""
+    _reduce_and_check(pp, oracle, cuda, dtype, op, np.array(lens, dtype=np.int64))
+
+
 @pytest.mark.parametrize("dtype", ["f32", "i32", "u64", "f64"])
 # rows of >= 256 elements go one warp per row (vector steps when rows are 16-byte
 # multiples, scalar otherwise); shorter rows, and few rows longer than 65536,
