@@ -212,11 +212,24 @@ def check_max_scan(torch, d_in, d_out, chunk: int = 1 << 27) -> bool:
     return True
 
 
+def release_cached_memory(torch) -> None:
+    """Return torch's cached device memory to the driver, then let the driver
+    finish reclaiming it before anything is timed: on GB300 the 2^28-element
+    scans that followed the release of 16 GiB ran 25-30 % slow for the next
+    few milliseconds (4 GiB: about a millisecond) and at full speed after a
+    pause of one second."""
+    torch.cuda.synchronize()
+    before = torch.cuda.memory_reserved()
+    torch.cuda.empty_cache()
+    freed = before - torch.cuda.memory_reserved()
+    if freed > (1 << 30):
+        time.sleep(min(2.0, 0.1 * freed / (1 << 30)))
+
+
 def time_device(torch, fn, steps: int, warmup: int, stream) -> tuple[float, list[float]]:
     """Run fn() warmup + steps times on `stream`; return (total ms of the timed
     steps bracketed by barrier + synchronize, per-launch ms from events)."""
-    torch.cuda.synchronize()
-    torch.cuda.empty_cache()
+    release_cached_memory(torch)
     for _ in range(warmup):
         fn()
     torch.cuda.synchronize()
@@ -271,8 +284,8 @@ def run_ours(args) -> dict | None:
     total = int(d_in.sum(dtype=torch.int64).item()) & 0xFFFFFFFF  # no converted copy of the input
     verified = (int(d_out[-1].item()) & 0xFFFFFFFF) == total and int(d_out[0].item()) == int(d_in[0].item())
     # free torch's cached scratch of that check (a large cached but unused block slowed the timed scans by ~3%
-    # on GB300)
-    torch.cuda.empty_cache()
+    # on GB300), and let the driver reclaim it
+    release_cached_memory(torch)
 
     vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0]
     gpu_index = int(vis) if vis.isdigit() else local
@@ -289,7 +302,7 @@ def run_ours(args) -> dict | None:
     h_timed = torch.empty(n, dtype=torch.int32, pin_memory=True) if (rank == 0 and not args.no_cpu_baseline) else None
     if h_timed is not None:
         h_timed.copy_(d_out)
-    torch.cuda.empty_cache()
+    release_cached_memory(torch)
     total_ms = max_over_ranks(torch, total_ms)
     ms_per_step = total_ms / args.steps
     value = ws * algo_bytes * args.steps / (total_ms * 1e-3) / 1e9
@@ -618,7 +631,7 @@ def bench_precision(torch, pp, stream, steps, gen) -> dict:
         d["compensated_slowdown_vs_plain"] = round(d["default"]["gbs"] / d["compensated"]["gbs"] - 1, 4)
         res[dist] = d
         del x, ref, cabs
-        torch.cuda.empty_cache()
+        release_cached_memory(torch)
     del outs
     return res
 
@@ -953,6 +966,40 @@ def run_profile_cases(args) -> dict:
     return {"profile_cases": cases}
 
 
+def run_profile_segmented(args) -> dict:
+    """The batched benchmark's segments (65,536 log-uniform lengths, 385 M
+    int32 elements): three segmented reductions, then three segmented scans,
+    no timing: the command of the launch-list capture in profiles/."""
+    import torch
+
+    import ppbuild
+
+    ppbuild.build()
+    import ppgb300 as pp
+
+    pp.lib()
+    sh = torch.cuda.current_stream().cuda_stream
+    S = 65536
+    g = torch.Generator(device="cpu").manual_seed(0x5EC)
+    lens = torch.floor(torch.exp(torch.rand(S, generator=g, dtype=torch.float64) * math.log(2 ** 16)))
+    offs = torch.zeros(S + 1, dtype=torch.int64)
+    offs[1:] = torch.cumsum(lens.clamp(1, 2 ** 16).to(torch.int64), 0)
+    n = int(offs[-1])
+    d_off = offs.cuda()
+    x = splitmix_u32(torch, SEED + 4, n, 0, 1000, "cuda")
+    y = torch.empty_like(x)
+    tot = torch.empty(S, dtype=torch.int32, device="cuda")
+    for _ in range(3):
+        pp.segmented_reduce("plus", x.data_ptr(), n, d_off.data_ptr(), S, tot.data_ptr(), "i32", stream=sh)
+    for _ in range(3):
+        pp.segmented_scan("inclusive", "plus", x.data_ptr(), y.data_ptr(), n, d_off.data_ptr(), S, "i32", stream=sh)
+    torch.cuda.synchronize()
+    if pp.stream_status(sh) != 0:
+        raise RuntimeError("device error in the segmented profile case")
+    ok = check_segmented_reduce(torch, x, tot, d_off) and check_segmented_scan(torch, x, y, d_off)
+    return {"profile_segmented": {"segments": S, "elements": n, "verified": bool(ok)}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -966,9 +1013,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-cases", action="store_true",
                     help="run each kernel of the path once on a small case (the ncu capture command)")
+    ap.add_argument("--profile-segmented", action="store_true",
+                    help="three segmented reductions and scans of the batched benchmark's segments, untimed")
     args = ap.parse_args()
     if args.profile_cases:
         print(json.dumps(run_profile_cases(args)), flush=True)
+        return
+    if args.profile_segmented:
+        print(json.dumps(run_profile_segmented(args)), flush=True)
         return
     if args.warmup < 3:
         args.warmup = 3

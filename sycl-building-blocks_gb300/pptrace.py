@@ -57,7 +57,11 @@ def summarise(raw: np.ndarray) -> dict:
     a = raw.reshape(-1, SLOTS).astype(np.int64)
     full, aggpub, lbdone, sstart, sdone = a[:, 0], a[:, 1], a[:, 3], a[:, 5], a[:, 6]
     cta, ticket, issue, rwait, rgot, pwait, pollrt = a[:, 8], a[:, 9], a[:, 10], a[:, 11], a[:, 12], a[:, 13], a[:, 14]
-    ok = (full > 0) & (aggpub > 0) & (lbdone > 0) & (sdone > 0) & (issue > 0) & (rgot > 0) & (pwait > 0)
+    # segmented reductions record no look-back events: their tiles are independent
+    has_lb = bool((lbdone > 0).any())
+    ok = (aggpub > 0) & (sdone > 0) & (issue > 0) & (rgot > 0) & (pwait > 0)
+    if has_lb:
+        ok &= (full > 0) & (lbdone > 0)
     ok[:300] = False
     ok[-300:] = False
     if ok.sum() < 10:
@@ -73,8 +77,8 @@ def summarise(raw: np.ndarray) -> dict:
         "issue_to_data_at_compute": q(rgot - issue),
         "compute_waits_for_data": q(rgot - rwait),
         "reduce_pass": q(aggpub - rgot),
-        "look_back_from_data_in": q(lbdone - full),
-        "prefix_known_after_own_aggregate": q(lbdone - aggpub),
+        "look_back_from_data_in": q(lbdone - full) if has_lb else None,
+        "prefix_known_after_own_aggregate": q(lbdone - aggpub) if has_lb else None,
         "compute_waits_for_prefix": q(sstart - pwait),
         "scan_pass": q(sdone - sstart),
         "stage_life (issue to scan done)": q(sdone - issue),
