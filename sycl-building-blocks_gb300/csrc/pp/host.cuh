@@ -520,8 +520,26 @@ struct SegWsLayout {
   size_t bitmap_off, bitmap_bytes, nonempty_off, rank_off, rank_out_off;
   size_t tile_base_off, tile_rec_off, tile_rec_bytes;  // reduce: per-tile base ranks and records
   size_t chunk_v_off, chunk_c_off;                     // reduce: per-chunk summaries of the records
+  size_t block_count_off;                              // reduce: non-empty segments per pre-pass block
   size_t scratch_bytes;
 };
+
+// Blocks of the reduce's pre-passes over segments (segment_heads_count_kernel,
+// segment_rank_kernel): at most 1,024 blocks of 256 threads, each thread a run
+// of per_thread consecutive segments.
+struct SegPrepassGrid {
+  uint64_t blocks, per_thread;
+};
+inline SegPrepassGrid seg_prepass_grid(uint64_t num_segments) {
+  const uint64_t threads = num_segments < 262144 ? (num_segments + 255) / 256 * 256 : 262144;
+  SegPrepassGrid g;
+  g.per_thread = (num_segments + threads - 1) / threads;
+  if (g.per_thread < 1) g.per_thread = 1;
+  const uint64_t used_threads = (num_segments + g.per_thread - 1) / g.per_thread;
+  g.blocks = (used_threads + 255) / 256;
+  if (g.blocks < 1) g.blocks = 1;
+  return g;
+}
 template <class T, class Op>
 inline SegWsLayout seg_ws_layout(uint64_t n, uint64_t num_segments, bool csr, bool reduce) {
   // sized for every variant a call may take
@@ -561,6 +579,8 @@ inline SegWsLayout seg_ws_layout(uint64_t n, uint64_t num_segments, bool csr, bo
   if (reduce) off += align_up(nchunks * sizeof(T), 256);
   L.chunk_c_off = off;
   if (reduce) off += align_up(nchunks * 4, 256);
+  L.block_count_off = off;
+  if (reduce) off += align_up(1024 * 4, 256);
   L.scratch_bytes = off;
   return L;
 }
@@ -578,7 +598,9 @@ inline Status acquire_scratch(cudaStream_t s, size_t need, unsigned char** out) 
 struct SegReduceExtra {
   const int64_t* offsets = nullptr;
   const uint32_t* nonempty = nullptr;
-  const uint32_t* rank = nullptr;
+  uint32_t* rank = nullptr;
+  const uint32_t* block_count = nullptr;  // from segment_heads_count_kernel
+  uint64_t prepass_blocks = 0, per_thread = 0;
   uint32_t* tile_base = nullptr;
   void* tile_rec = nullptr;
   size_t tile_rec_bytes = 0;
@@ -605,9 +627,10 @@ inline Status launch_segmented_variant(cudaStream_t s, const SegArgs& a0, uint64
     if (!rx || rx->tile_rec_bytes < ntiles * sizeof(SegTileRec<typename Pol::in_t>)) return Status::workspace;
     a.tile_base = rx->tile_base;
     a.tile_rec = rx->tile_rec;
-    const unsigned tgrid = unsigned((ntiles + 7) / 8 < 4096 ? (ntiles + 7) / 8 : 4096);  // a warp per tile
-    segment_tile_base_kernel<<<tgrid, 256, 0, s>>>(rx->offsets, rx->nonempty, rx->rank, num_segments,
-                                                   uint64_t(Cfg::TILE), ntiles, rx->tile_base);
+    // ranks of the non-empty segments and the base rank of every tile of this variant
+    segment_rank_kernel<<<unsigned(rx->prepass_blocks), 256, 0, s>>>(rx->offsets, rx->nonempty, num_segments,
+                                                                       a0.s.n, rx->per_thread, rx->block_count,
+                                                                       uint64_t(Cfg::TILE), rx->rank, rx->tile_base);
     if (cudaGetLastError() != cudaSuccess) return Status::cuda;
     if (cudaMemsetAsync(rx->tile_rec, 0, ntiles * sizeof(SegTileRec<typename Pol::in_t>), s) != cudaSuccess)
       return Status::cuda;
@@ -710,11 +733,13 @@ inline Status segmented_reduce(cudaStream_t s, const T* in, uint64_t n, const in
   T* by_rank = reinterpret_cast<T*>(base + L.rank_out_off);
   if (cudaMemsetAsync(heads, 0, L.bitmap_bytes, s) != cudaSuccess) return Status::cuda;
   const unsigned pre_grid = unsigned((num_segments + 255) / 256 < 1024 ? (num_segments + 255) / 256 : 1024);
-  segment_heads_kernel<T, Op><<<pre_grid, 256, 0, s>>>(offsets, num_segments, n, heads, nonempty, out);
+  // heads, flags and identities in contiguous blocks, then ranks from the blocks' counts
+  const SegPrepassGrid pg = seg_prepass_grid(num_segments);
+  uint32_t* block_count = reinterpret_cast<uint32_t*>(base + L.block_count_off);
+  segment_heads_count_kernel<T, Op><<<unsigned(pg.blocks), 256, 0, s>>>(offsets, num_segments, n, pg.per_thread,
+                                                                         heads, nonempty, out, block_count);
   if (cudaGetLastError() != cudaSuccess) return Status::cuda;
   if (n == 0) return Status::ok;
-  st = decoupled_scan<PlainScan<uint32_t, plus>>(s, nonempty, rank, num_segments, true, w.hdr, L.control_bytes);
-  if (st != Status::ok) return st;
   SegArgs a{};
   a.s.in = in;
   a.s.out = nullptr;
@@ -729,6 +754,9 @@ inline Status segmented_reduce(cudaStream_t s, const T* in, uint64_t n, const in
   rx.offsets = offsets;
   rx.nonempty = nonempty;
   rx.rank = rank;
+  rx.block_count = block_count;
+  rx.prepass_blocks = pg.blocks;
+  rx.per_thread = pg.per_thread;
   rx.tile_base = reinterpret_cast<uint32_t*>(base + L.tile_base_off);
   rx.tile_rec = base + L.tile_rec_off;
   rx.tile_rec_bytes = L.tile_rec_bytes;

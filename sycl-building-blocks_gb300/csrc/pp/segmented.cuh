@@ -798,35 +798,101 @@ __global__ void segment_heads_kernel(const int64_t* offsets, uint64_t num_segmen
   }
 }
 
-// Segmented reduce, before the main kernel: base[t] = the non-empty segments
-// that start before tile t (t * tile): one warp per tile finds the first
-// segment with offsets[s] >= t * tile by a 32-way search (about four dependent
-// loads for 2^16 segments, instead of sixteen for a binary search) and reads
-// the exclusive scan of the non-empty flags (`rank`) there. (A template only so
-// that every translation unit including this header may instantiate it.)
-template <class Index = int64_t>
-__global__ void segment_tile_base_kernel(const Index* offsets, const uint32_t* nonempty, const uint32_t* rank,
-                                         uint64_t num_segments, uint64_t tile, uint64_t ntiles, uint32_t* base) {
+// Segmented reduce, first pass (segment_heads_kernel for reductions): block b
+// of the grid takes the contiguous segments [b * 256 * per_thread, (b + 1) *
+// 256 * per_thread), each thread `per_thread` consecutive ones; it writes the
+// head bitmap, the non-empty flags and the identity of every empty segment,
+// and the block's count of non-empty segments to block_count[b].
+template <class T, class Op>
+__global__ void __launch_bounds__(256) segment_heads_count_kernel(const int64_t* offsets, uint64_t num_segments,
+                                                                  uint64_t n, uint64_t per_thread, uint32_t* heads,
+                                                                  uint32_t* nonempty, T* reduce_out,
+                                                                  uint32_t* block_count) {
+  __shared__ uint32_t s_w[8];
+  const uint64_t s0 = (uint64_t(blockIdx.x) * 256 + threadIdx.x) * per_thread;
+  uint32_t cnt = 0;
+  for (uint64_t s = s0; s < s0 + per_thread && s < num_segments; ++s) {
+    int64_t b = offsets[s], e = offsets[s + 1];
+    if (b < 0) b = 0;
+    if (e > int64_t(n)) e = int64_t(n);
+    const bool ne = e > b;
+    nonempty[s] = ne ? 1u : 0u;
+    cnt += ne ? 1u : 0u;
+    if (ne) atomicOr(heads + (uint64_t(b) >> 5), 1u << (uint64_t(b) & 31));
+    if (!ne) reduce_out[s] = identity<Op, T>();
+  }
   const int lane = threadIdx.x & 31;
-  const uint64_t warps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
-  for (uint64_t t = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5; t < ntiles; t += warps) {
-    const Index target = Index(t * tile);
-    uint64_t lo = 0, hi = num_segments;  // answer in [lo, hi]
-    while (hi - lo > 32) {
-      const uint64_t step = (hi - lo + 31) / 32;
-      const uint64_t probe = lo + uint64_t(lane) * step;  // offsets[probe] < target for the lanes below the answer
-      const bool below = probe < hi && offsets[probe] < target;
-      const uint32_t m = __ballot_sync(kFullMask, below);
-      const int k = __popc(m);  // lanes 0 .. k-1 are below
-      const uint64_t nlo = k == 0 ? lo : lo + uint64_t(k - 1) * step + 1;
-      const uint64_t nhi = lo + uint64_t(k) * step < hi ? lo + uint64_t(k) * step : hi;
-      lo = nlo;
-      hi = nhi;
+  cnt = warp_reduce(cnt, plus{}, lane);
+  if (lane == 0) s_w[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int i = 0; i < 8; ++i) t += s_w[i];
+    block_count[blockIdx.x] = t;
+  }
+}
+
+// Segmented reduce, second pass: rank[s] = the non-empty segments before s
+// (the exclusive scan of the flags), over the blocks of
+// segment_heads_count_kernel: a block adds up the counts of the blocks before
+// it (at most 1,024) and scans its own flags in order. It also writes base[t],
+// the non-empty segments that start before tile t: the non-empty segments
+// cover [0, n) without gaps, so every tile start t * tile lies in exactly one
+// of them, [a, b), and base[t] is that segment's rank, plus one when the
+// segment starts before the tile. A segment covering more than 32 tile starts
+// has them written by its whole warp. (A template only so that every
+// translation unit including this header may instantiate it.)
+template <class Index = int64_t>
+__global__ void __launch_bounds__(256) segment_rank_kernel(const Index* offsets, const uint32_t* nonempty,
+                                                           uint64_t num_segments, uint64_t n, uint64_t per_thread,
+                                                           const uint32_t* block_count, uint64_t tile,
+                                                           uint32_t* rank, uint32_t* base) {
+  __shared__ uint32_t s_w[8];
+  __shared__ uint32_t s_base;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t before = 0;
+  for (uint32_t bk = threadIdx.x; bk < blockIdx.x; bk += 256) before += block_count[bk];
+  before = warp_reduce(before, plus{}, lane);
+  if (lane == 0) s_w[w] = before;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int i = 0; i < 8; ++i) t += s_w[i];
+    s_base = t;
+  }
+  __syncthreads();
+  const uint64_t s0 = (uint64_t(blockIdx.x) * 256 + threadIdx.x) * per_thread;
+  uint32_t cnt = 0;
+  for (uint64_t s = s0; s < s0 + per_thread && s < num_segments; ++s) cnt += nonempty[s];
+  const uint32_t inc = warp_inclusive_scan(cnt, plus{}, lane);
+  if (lane == 31) s_w[w] = inc;
+  __syncthreads();
+  uint32_t r = s_base + inc - cnt;
+  for (int i = 0; i < w; ++i) r += s_w[i];
+  for (uint64_t i = 0; i < per_thread; ++i) {  // the same trip count in every lane
+    const uint64_t s = s0 + i;
+    uint64_t t0 = 0, t1 = 0;  // tile starts in [t0, t1) lie in this segment
+    int64_t a = 0;
+    if (s < num_segments) {
+      rank[s] = r;
+      if (nonempty[s]) {
+        a = int64_t(offsets[s]) < 0 ? 0 : int64_t(offsets[s]);
+        const int64_t e = int64_t(offsets[s + 1]) > int64_t(n) ? int64_t(n) : int64_t(offsets[s + 1]);
+        t0 = (uint64_t(a) + tile - 1) / tile;
+        t1 = (uint64_t(e) + tile - 1) / tile;
+      }
     }
-    const uint64_t probe = lo + uint64_t(lane);
-    const bool below = probe < hi && offsets[probe] < target;
-    const uint64_t first = lo + uint64_t(__popc(__ballot_sync(kFullMask, below)));
-    if (lane == 0) base[t] = first < num_segments ? rank[first] : rank[num_segments - 1] + nonempty[num_segments - 1];
+    const bool long_run = t1 > t0 + 32;
+    if (!long_run)
+      for (uint64_t t = t0; t < t1; ++t) base[t] = r + (t * tile > uint64_t(a) ? 1u : 0u);
+    for (uint32_t m = __ballot_sync(kFullMask, long_run); m != 0u; m &= m - 1u) {
+      const int src = __ffs(m) - 1;
+      const uint64_t u0 = __shfl_sync(kFullMask, t0, src), u1 = __shfl_sync(kFullMask, t1, src);
+      const int64_t ua = __shfl_sync(kFullMask, a, src);
+      const uint32_t ur = __shfl_sync(kFullMask, r, src);
+      for (uint64_t t = u0 + lane; t < u1; t += 32) base[t] = ur + (t * tile > uint64_t(ua) ? 1u : 0u);
+    }
+    if (s < num_segments) r += nonempty[s];
   }
 }
 
