@@ -883,14 +883,44 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
         const int r0 = seg * Cfg::SEG + lane * (CH * V);
         const bool interior = g.lo == 0 && g.blo == 0 && g.bhi == TILE;
         row_info_t m = RF::id(pol);
+        if constexpr (RF::value) {
+          // the row's statistic first, then its total: from an offset that
+          // dominates every partial sum, with the policy's cheaper exact
+          // additions (compensated sums: FastTwoSum instead of TwoSum)
 #pragma unroll
-        for (int c = 0; c < CH; ++c) {
-          in_t x[V];
-          load_raw_at(s, r0 + c * V, g, interior, x);
+          for (int c = 0; c < CH; ++c) {
+            in_t x[V];
+            load_raw_at(s, r0 + c * V, g, interior, x);
 #pragma unroll
-          for (int j = 0; j < V; ++j) {
-            r = pol.aop_in(r, x[j]);
-            if constexpr (RF::value) m = RF::add(pol, m, x[j]);
+            for (int j = 0; j < V; ++j) m = RF::add(pol, m, x[j]);
+          }
+          const float off = pol.row_offset(m);
+          if (off != 0.0f) {
+            acc_t t{off, 0.0f};
+#pragma unroll
+            for (int c = 0; c < CH; ++c) {
+              in_t x[V];
+              load_raw_at(s, r0 + c * V, g, interior, x);
+#pragma unroll
+              for (int j = 0; j < V; ++j) pol.row_offset_add(t, x[j]);
+            }
+            r = pol.row_offset_total(t, off);
+          } else {
+#pragma unroll
+            for (int c = 0; c < CH; ++c) {
+              in_t x[V];
+              load_raw_at(s, r0 + c * V, g, interior, x);
+#pragma unroll
+              for (int j = 0; j < V; ++j) r = pol.aop_in(r, x[j]);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < CH; ++c) {
+            in_t x[V];
+            load_raw_at(s, r0 + c * V, g, interior, x);
+#pragma unroll
+            for (int j = 0; j < V; ++j) r = pol.aop_in(r, x[j]);
           }
         }
         info = m;

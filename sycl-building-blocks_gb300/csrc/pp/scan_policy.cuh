@@ -176,6 +176,25 @@ struct CompensatedF32 {
     r = ff32{s, __fadd_rn(r.lo, e)};
     return o;
   }
+  // Row totals (reduce pass) from the row's max|x| = m: starting the chain at
+  // P, a power of two with P >= 64 m, every running sum stays in [P/2, 2P]
+  // for rows of up to 31 elements, so each element enters with FastTwoSum
+  // (exact) and the total (s - P, lo) is exact too (s - P by Sterbenz's
+  // lemma). row_offset returns 0 where that cannot be used (m infinite, NaN
+  // or at least 2^120): those rows keep TwoSum.
+  __device__ __forceinline__ float row_offset(float m) const {
+    const uint32_t ex = (__float_as_uint(m) >> 23) & 0xFFu;  // m < 2^(ex - 126)
+    if (!(m < 0x1.0p120f)) return 0.0f;
+    return __uint_as_float((ex + 7u) << 23);  // 2^(ex - 120) >= 64 * 2^(ex - 126) > 64 m
+  }
+  __device__ __forceinline__ void row_offset_add(ff32& r, float x) const {
+    float s, e;
+    fast_two_sum(r.hi, x, s, e);
+    r = ff32{s, __fadd_rn(r.lo, e)};
+  }
+  __device__ __forceinline__ ff32 row_offset_total(const ff32& r, float p) const {
+    return ff32{__fsub_rn(r.hi, p), r.lo};
+  }
 };
 
 // Policies without a fast row path (kRowFast absent) see these defaults.
