@@ -886,33 +886,28 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
         if constexpr (RF::value) {
           // the row's statistic first, then its total: from an offset that
           // dominates every partial sum, with the policy's cheaper exact
-          // additions (compensated sums: FastTwoSum instead of TwoSum)
+          // additions (compensated sums: FastTwoSum instead of TwoSum); the
+          // row's elements stay in registers between the two
+          in_t xs[CH][V];
 #pragma unroll
           for (int c = 0; c < CH; ++c) {
-            in_t x[V];
-            load_raw_at(s, r0 + c * V, g, interior, x);
+            load_raw_at(s, r0 + c * V, g, interior, xs[c]);
 #pragma unroll
-            for (int j = 0; j < V; ++j) m = RF::add(pol, m, x[j]);
+            for (int j = 0; j < V; ++j) m = RF::add(pol, m, xs[c][j]);
           }
           const float off = pol.row_offset(m);
           if (off != 0.0f) {
             acc_t t{off, 0.0f};
 #pragma unroll
-            for (int c = 0; c < CH; ++c) {
-              in_t x[V];
-              load_raw_at(s, r0 + c * V, g, interior, x);
+            for (int c = 0; c < CH; ++c)
 #pragma unroll
-              for (int j = 0; j < V; ++j) pol.row_offset_add(t, x[j]);
-            }
+              for (int j = 0; j < V; ++j) pol.row_offset_add(t, xs[c][j]);
             r = pol.row_offset_total(t, off);
           } else {
 #pragma unroll
-            for (int c = 0; c < CH; ++c) {
-              in_t x[V];
-              load_raw_at(s, r0 + c * V, g, interior, x);
+            for (int c = 0; c < CH; ++c)
 #pragma unroll
-              for (int j = 0; j < V; ++j) r = pol.aop_in(r, x[j]);
-            }
+              for (int j = 0; j < V; ++j) r = pol.aop_in(r, xs[c][j]);
           }
         } else {
 #pragma unroll
