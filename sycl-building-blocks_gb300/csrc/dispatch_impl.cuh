@@ -25,7 +25,7 @@ Status scan_policy(const ScanReq& r) {
 
 template <class Pol>
 size_t workspace_policy(pp_scan_algo algo, const void* in, const void* out, uint64_t n) {
-  if (algo == PP_ALGO_COOPERATIVE) return workspace_bytes_for_desc_words(0);
+  if (algo == PP_ALGO_COOPERATIVE) return host::cooperative_workspace_bytes<Pol>(n, in, out);
   return host::decoupled_workspace_bytes<Pol>(n, in, out);
 }
 

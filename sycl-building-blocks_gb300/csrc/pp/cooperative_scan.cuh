@@ -8,9 +8,18 @@
 // barrier, lets every group fold the tails of all earlier chunks serially
 // (an O(G) fan per group), crosses a second barrier and re-reads and
 // re-writes the whole output to add the carry: about 4n memory traffic and a
-// 64-group limit (cooperative_groups.hpp:66-68). Here one cooperative launch
-// (all blocks co-resident, checked with the occupancy calculator before the
-// launch) runs:
+// 64-group limit (cooperative_groups.hpp:66-68).
+//
+// Element types whose size divides 16 bytes take the staged kernel of
+// decoupled_scan.cuh in cooperative rounds (CO = 1): the input streams
+// through L2 in windows of about 20 MB; each CTA reduces its run of window w
+// (first read, from HBM), publishes the run aggregate at window barrier w,
+// and scans its run of window w - 1 (second read, from L2) with the prefix of
+// all earlier runs: 2n HBM traffic, one split-phase grid barrier per window.
+//
+// This file holds the register-tile kernel for the other element types: one
+// cooperative launch (all blocks co-resident, checked with the occupancy
+// calculator before the launch) runs:
 //   1. each block reduces its contiguous run of tiles in sequence order and
 //      publishes the run aggregate;
 //   2. a bounded-spin grid barrier;

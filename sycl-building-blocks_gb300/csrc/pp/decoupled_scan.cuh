@@ -63,6 +63,13 @@ struct ScanArgs {
   // quarter of that, and counts look-back outcomes in WsHeader::dbg.
   uint32_t debug_delay_ns = 0;
   uint32_t debug_seed = 0;
+  // Cooperative rounds of the staged kernel (CO = 1): tiles per CTA per
+  // window, the window aggregate slots (4 x gridDim.x slots of 16 bytes) and
+  // the L2 priority of the first read of a window (0: evict_normal,
+  // 1: evict_last).
+  int coop_kt = 0;
+  int coop_l2 = 0;
+  void* coop_aggs = nullptr;
 };
 
 // Pseudo-random delay in [0, max_ns] for event `ev` of `tile` (a 32-bit
@@ -284,7 +291,7 @@ struct pol_commutative<F64CarryF32> : std::true_type {};
 // 16-byte bank groups for any 8 consecutive lanes, so row reads are free of
 // bank conflicts; results go back into the row and leave striped or by bulk
 // copy.
-template <class Pol, int NC_, int CH_, int STAGES_, int LBW_, int LAY_ = 0, int SW_ = 0>
+template <class Pol, int NC_, int CH_, int STAGES_, int LBW_, int LAY_ = 0, int SW_ = 0, int CO_ = 0>
 struct StagedCfg {
   using in_t = typename Pol::in_t;
   using acc_t = typename Pol::acc_t;
@@ -302,18 +309,42 @@ struct StagedCfg {
   static constexpr int TILE = NC * SEG;
   static constexpr int TILE_BYTES = TILE * int(sizeof(in_t));
   static constexpr int SW = SW_;            // store warps (1: a warp writes finished tiles back by bulk copy)
-  static constexpr int THREADS = (NC + 2 + SW) * 32;
+  static constexpr int CO = CO_;            // cooperative rounds: one more warp (window barriers and folds)
+  static constexpr int THREADS = (NC + 2 + SW + (CO_ != 0 ? 1 : 0)) * 32;
   // per-stage metadata
   static constexpr size_t META_AGG = 0;  // acc_t[NC] segment aggregates, then their exclusive prefixes
   static constexpr size_t META_PREF = align_up(NC * sizeof(acc_t), 16);   // carry_t tile exclusive prefix
   static constexpr size_t META_TAGG = META_PREF + align_up(sizeof(carry_t), 16);  // carry_t tile aggregate
   static constexpr size_t META_TILE = META_TAGG + align_up(sizeof(carry_t), 8);   // long long tile index
   static constexpr size_t META_CNT = META_TILE + 8;                                // unsigned arrivals
-  static constexpr size_t META_ROWS = align_up(META_CNT + 4, 16);  // acc_t[NC*32] row prefixes in the segment
+  static constexpr size_t META_JOB = META_CNT + 4;  // unsigned: 1 = a scan job of the cooperative rounds
+  static constexpr size_t META_ROWS = align_up(META_JOB + 4, 16);  // acc_t[NC*32] row prefixes in the segment
   static constexpr size_t META_BYTES = align_up(META_ROWS + (LAY_ == 2 ? NC_ * 32 * sizeof(acc_t) : 0), 16);
+  // cooperative rounds: per-tile record of REC_WORDS 64-bit words, the
+  // 32-bit words of the tile aggregate (carry_t) and of the NC segment
+  // exclusive prefixes (acc_t) in their low halves. The high halves stay 0:
+  // the records live where look-back descriptors live, and a word with a 0
+  // tag reads as an invalid descriptor that any later publication overwrites.
+  static constexpr int REC_CW = words<carry_t>::W;
+  static constexpr int REC_AW = words<acc_t>::W;
+  static constexpr int REC_WORDS = REC_CW + NC * REC_AW;
+  static constexpr size_t REC_BYTES = align_up(size_t(REC_WORDS) * 8, 16);
   static constexpr size_t OFF_META = size_t(STAGES) * TILE_BYTES;
   static constexpr size_t OFF_BAR = align_up(OFF_META + STAGES * META_BYTES, 8);  // 5 barriers / stage
-  static constexpr size_t SMEM = OFF_BAR + 5 * STAGES * 8;
+  // cooperative rounds: carry_t run aggregates by window parity, carry_t
+  // window prefixes by window parity, two counters, two mbarriers, then the
+  // ring that hands scan jobs their prefixes: RING slots of {carry_t tile
+  // prefix in 16 bytes, acc_t[NC] segment prefixes} with a full and a free
+  // mbarrier each
+  static constexpr int RING = 2;
+  static constexpr size_t RING_SLOT = 16 + align_up(NC * sizeof(acc_t), 16);
+  static constexpr size_t OFF_CO = align_up(OFF_BAR + 5 * STAGES * 8, 16);
+  static constexpr size_t CO_WAGG = OFF_CO;
+  static constexpr size_t CO_WIN = OFF_CO + 32;
+  static constexpr size_t CO_CNT = OFF_CO + 64;  // unsigned reduce jobs done, unsigned windows taken
+  static constexpr size_t CO_BAR = OFF_CO + 80;  // 2 window mbarriers, then RING full and RING free
+  static constexpr size_t CO_RING = align_up(CO_BAR + (2 + 2 * RING) * 8, 16);
+  static constexpr size_t SMEM = CO_ != 0 ? CO_RING + RING * RING_SLOT : OFF_BAR + 5 * STAGES * 8;
 };
 
 // Geometry of tile t in the staged kernel. The tile grid is shifted by `head`
@@ -588,6 +619,139 @@ __device__ __forceinline__ bool lookback_pipelined(const Pol& pol, const uint64_
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// Cooperative rounds (CO = 1): the grid-barrier scan of scan_cooperative.hpp
+// with the input streamed through L2 in windows. The tiles are cut into
+// windows of gridDim.x * coop_kt tiles; window w is split into one contiguous
+// run per CTA, in block order. Round r of a CTA reduces its run of window r
+// (a first read from HBM, which leaves the window in L2) and publishes the run
+// aggregate at window barrier r, then scans its run of window r - 1 (a second
+// read, served by L2) with the prefix of all earlier runs. The barrier is
+// split: arriving never waits, and the wait for barrier r - 1 comes a whole
+// window of reduce work after this CTA's own arrival there, so CTAs only stall
+// when one falls a round behind. HBM sees each element read once and written
+// once (2n) instead of the 3n of reduce, barrier, re-read.
+struct CoopRuns {
+  long long ntiles, G, b, kt, R;  // R windows
+  __device__ __forceinline__ CoopRuns(long long ntiles_, long long G_, long long b_, long long kt_)
+      : ntiles(ntiles_), G(G_), b(b_), kt(kt_), R((ntiles_ + G_ * kt_ - 1) / (G_ * kt_)) {}
+  // tiles [t0, t1) of this CTA in window w (the last window may be partial:
+  // its runs differ by at most one tile)
+  __device__ __forceinline__ void run(long long w, long long& t0, long long& t1) const {
+    const long long base = w * G * kt;
+    const long long rem = (ntiles - base < G * kt) ? ntiles - base : G * kt;
+    const long long q = rem / G, r = rem % G;
+    t0 = base + b * q + (b < r ? b : r);
+    t1 = t0 + q + (b < r ? 1 : 0);
+  }
+};
+
+// The job sequence of one CTA: (tile, scan?) pairs, round by round.
+struct CoopCursor {
+  CoopRuns runs;
+  long long r = 0, t = 0, e = 0;
+  int part = 0;  // 0: reduce jobs of window r, 1: scan jobs of window r - 1
+  __device__ __forceinline__ explicit CoopCursor(const CoopRuns& rr) : runs(rr) { runs.run(0, t, e); }
+  __device__ __forceinline__ bool next(long long& tile, bool& scan) {
+    while (t >= e) {
+      if (part == 0) {
+        part = 1;
+        if (r >= 1) {
+          runs.run(r - 1, t, e);
+        } else {
+          t = e = 0;
+        }
+      } else {
+        ++r;
+        part = 0;
+        if (r > runs.R) return false;
+        if (r < runs.R) {
+          runs.run(r, t, e);
+        } else {
+          t = e = 0;
+        }
+      }
+    }
+    tile = t++;
+    scan = part == 1;
+    return true;
+  }
+};
+
+// Window aggregate slots: 16 bytes each, written by lane 0 with plain stores
+// before the fence and the arrival, read with volatile word loads after an
+// acquire of the arrival counter.
+template <class C>
+__device__ __forceinline__ void coop_store_slot(C* slot, const C& v) {
+  const words<C> w = to_words(v);
+  volatile uint32_t* p = reinterpret_cast<volatile uint32_t*>(slot);
+#pragma unroll
+  for (int i = 0; i < words<C>::W; ++i) p[i] = w.w[i];
+}
+template <class C>
+__device__ __forceinline__ C coop_load_slot(const C* slot) {
+  words<C> w;
+  const volatile uint32_t* p = reinterpret_cast<const volatile uint32_t*>(slot);
+#pragma unroll
+  for (int i = 0; i < words<C>::W; ++i) w.w[i] = p[i];
+  return from_words<C>(w);
+}
+
+// Whole-warp bounded wait until *ctr >= target (every lane acquires the
+// counter itself). False after a timeout (recorded, detail = the window) or
+// when another CTA aborted.
+__device__ __forceinline__ bool coop_wait_arrivals(WsHeader* h, const unsigned long long* ctr,
+                                                   unsigned long long target, uint64_t timeout_ns,
+                                                   unsigned long long detail, int lane) {
+  uint64_t t0 = 0;
+  for (uint32_t it = 0;; ++it) {
+    const unsigned long long v = ptx::ld_acquire(reinterpret_cast<const uint64_t*>(ctr));
+    if (__all_sync(kFullMask, v >= target)) return true;
+    if (it == 0) t0 = ptx::globaltimer_ns();
+    if ((it & 15u) == 15u) {
+      int stop = 0;
+      if (lane == 0) {
+        if (aborted(h)) {
+          stop = 1;
+        } else if (ptx::globaltimer_ns() - t0 > timeout_ns) {
+          raise_error(h, kDevTimeout, detail);
+          stop = 1;
+        }
+      }
+      if (__shfl_sync(kFullMask, stop, 0)) return false;
+    }
+  }
+}
+
+// Whole-warp bounded wait until the shared counter *cnt >= target (then an
+// acquire fence at CTA scope). False after a timeout (recorded) or when
+// another CTA aborted.
+__device__ __forceinline__ bool coop_wait_smem_count(WsHeader* h, const unsigned* cnt, unsigned target,
+                                                     uint64_t timeout_ns, unsigned long long detail, int lane) {
+  uint64_t t0 = 0;
+  for (uint32_t it = 0;; ++it) {
+    const unsigned v = *reinterpret_cast<const volatile unsigned*>(cnt);
+    if (__all_sync(kFullMask, v >= target)) {
+      __threadfence_block();
+      return true;
+    }
+    if (it == 0) t0 = ptx::globaltimer_ns();
+    if (it >= 4) ptx::nanosleep(64);
+    if ((it & 15u) == 15u) {
+      int stop = 0;
+      if (lane == 0) {
+        if (aborted(h)) {
+          stop = 1;
+        } else if (ptx::globaltimer_ns() - t0 > timeout_ns) {
+          raise_error(h, kDevTimeout, detail);
+          stop = 1;
+        }
+      }
+      if (__shfl_sync(kFullMask, stop, 0)) return false;
+    }
+  }
+}
+
 // Every compute warp runs the reduce pass of tile k+1 before the scan pass of
 // tile k, so the next aggregate is published before this CTA waits for a
 // prefix.
@@ -601,11 +765,14 @@ __device__ __forceinline__ bool lookback_pipelined(const Pol& pol, const uint64_
 // Later tickets make the order of tickets follow the order in which tiles
 // reach their reduce pass more closely, so predecessors' aggregates arrive
 // closer together; earlier ones hide the latency of the ticket atomic.
+// CO: 0 = decoupled look-back (tickets, descriptors); 1 = cooperative rounds
+// (a cooperative launch; warp 1 runs the window barriers and the carry chain
+// of this CTA's tiles instead of the look-back).
 template <class Pol, int NC, int CH, int STAGES, int LBW, int LAY = 0, int TK = 0, unsigned PG = 0, int BS = 0,
-          class Trace = NoTrace>
-__global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
+          class Trace = NoTrace, int CO = 0>
+__global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0) + (CO != 0 ? 1 : 0)) * 32, 1)
     decoupled_staged_kernel(const ScanArgs args) {
-  using Cfg = StagedCfg<Pol, NC, CH, STAGES, LBW, LAY, (BS == 2 ? 1 : 0)>;
+  using Cfg = StagedCfg<Pol, NC, CH, STAGES, LBW, LAY, (BS == 2 ? 1 : 0), CO>;
   static_assert(TK == 0 || TK == 2, "tickets a stage life ahead (0) or once the stage is free (2)");
   static_assert(BS == 0 || (BS == 2 && LAY == 2), "the store warp serves the rows layout");
   using in_t = typename Pol::in_t;
@@ -631,6 +798,18 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
   auto s_tagg = [&](int s) { return reinterpret_cast<carry_t*>(meta(s) + Cfg::META_TAGG); };
   auto s_tile = [&](int s) { return reinterpret_cast<long long*>(meta(s) + Cfg::META_TILE); };
   auto s_cnt = [&](int s) { return reinterpret_cast<unsigned*>(meta(s) + Cfg::META_CNT); };
+  auto s_job = [&](int s) { return reinterpret_cast<unsigned*>(meta(s) + Cfg::META_JOB); };
+  // cooperative rounds (unused otherwise): run aggregates and window prefixes
+  // by window parity; co_cnt[0] = reduce jobs done, co_cnt[1] = windows whose
+  // prefix warp 1 has taken; co_winb[p]: the prefix of a window of parity p
+  // is in co_win[p]
+  carry_t* co_wagg = reinterpret_cast<carry_t*>(smem + Cfg::CO_WAGG);
+  carry_t* co_win = reinterpret_cast<carry_t*>(smem + Cfg::CO_WIN);
+  unsigned* co_cnt = reinterpret_cast<unsigned*>(smem + Cfg::CO_CNT);
+  uint64_t* co_winb = reinterpret_cast<uint64_t*>(smem + Cfg::CO_BAR);
+  uint64_t* co_rfull = co_winb + 2;
+  uint64_t* co_rfree = co_winb + 2 + Cfg::RING;
+  auto co_slot = [&](int d) { return smem + Cfg::CO_RING + size_t(d) * Cfg::RING_SLOT; };
   auto s_rows = [&](int s) { return reinterpret_cast<acc_t*>(meta(s) + Cfg::META_ROWS); };
 
   const Pol pol{};
@@ -656,6 +835,18 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
       ptx::mbar_init(&prefb[s], 1);
       *s_cnt(s) = 0u;
     }
+    if constexpr (CO != 0) {
+      for (int p = 0; p < 2; ++p) {
+        ptx::mbar_init(&co_winb[p], 1);
+        co_wagg[p] = Pol{}.cid();
+      }
+      for (int d = 0; d < Cfg::RING; ++d) {
+        ptx::mbar_init(&co_rfull[d], 1);
+        ptx::mbar_init(&co_rfree[d], NC);
+      }
+      co_cnt[0] = 0u;
+      co_cnt[1] = 0u;
+    }
     ptx::fence_mbar_init();
   }
   __syncthreads();
@@ -667,46 +858,201 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
       const uint64_t pol_l2 = ptx::policy_evict_first();
       const unsigned char* in = static_cast<const unsigned char*>(args.in);
       uint32_t pending = 0, pend_par = 0;
-      auto draw = [&]() {
-        const long long x = (long long)atomicAdd(&hdr->ticket, 1ull);
-        if (x < ntiles) trace_now(kTrTicket, x);
-        return x;
-      };
-      long long t = TK == 0 ? draw() : 0;
-      for (int k = 0;; ++k) {
-        const int s = k % STAGES;
-        if (k >= STAGES) {
-          const uint32_t par = ((k / STAGES) - 1) & 1;
-          if (!mbar_wait_bounded(&empty[s], par, hdr, tmo, (unsigned long long)t)) break;
-          if constexpr (TK == 2) t = draw();
-          pending &= ~(1u << s);
-        } else if constexpr (TK != 0) {
-          t = draw();
-        }
-        *s_tile(s) = t;
-        if (t < ntiles) {
-          trace_now(kTrIssue, t);
-          const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(t, n, head);
-          const uint32_t bytes = uint32_t(g.bhi - g.blo) * uint32_t(sizeof(in_t));
-          if (bytes) {
-            ptx::mbar_arrive_expect_tx(&full[s], bytes);
-            ptx::bulk_g2s(smem + size_t(s) * Cfg::TILE_BYTES + size_t(g.blo) * sizeof(in_t),
-                          in + (g.gbase + g.blo) * (long long)sizeof(in_t), bytes, &full[s], pol_l2);
-            pending |= 1u << s;
-            pend_par = (pend_par & ~(1u << s)) | ((uint32_t(k / STAGES) & 1u) << s);
-          } else {
-            ptx::mbar_arrive(&full[s]);
-          }
-          if constexpr (TK == 0) t = draw();
+      // bulk copy of tile t into stage s (use k)
+      auto issue = [&](int s, int k, long long t, uint64_t l2) {
+        trace_now(kTrIssue, t);
+        const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(t, n, head);
+        const uint32_t bytes = uint32_t(g.bhi - g.blo) * uint32_t(sizeof(in_t));
+        if (bytes) {
+          ptx::mbar_arrive_expect_tx(&full[s], bytes);
+          ptx::bulk_g2s(smem + size_t(s) * Cfg::TILE_BYTES + size_t(g.blo) * sizeof(in_t),
+                        in + (g.gbase + g.blo) * (long long)sizeof(in_t), bytes, &full[s], l2);
+          pending |= 1u << s;
+          pend_par = (pend_par & ~(1u << s)) | ((uint32_t(k / STAGES) & 1u) << s);
         } else {
           ptx::mbar_arrive(&full[s]);
-          break;
+        }
+      };
+      if constexpr (CO != 0) {
+        // the first read of a window stays in L2 for the second (scan) read,
+        // which is its last use
+        const uint64_t pol_keep = args.coop_l2 ? ptx::policy_evict_last() : ptx::policy_evict_normal();
+        CoopCursor cur(CoopRuns(ntiles, gridDim.x, blockIdx.x, args.coop_kt));
+        for (int k = 0;; ++k) {
+          const int s = k % STAGES;
+          if (k >= STAGES) {
+            const uint32_t par = ((k / STAGES) - 1) & 1;
+            if (!mbar_wait_bounded(&empty[s], par, hdr, tmo, 0ull)) break;
+            pending &= ~(1u << s);
+          }
+          long long t = 0;
+          bool scan = false;
+          const bool more = cur.next(t, scan);
+          *s_tile(s) = more ? t : ntiles;
+          *s_job(s) = scan ? 1u : 0u;
+          if (!more) {
+            ptx::mbar_arrive(&full[s]);
+            break;
+          }
+          issue(s, k, t, scan ? pol_l2 : pol_keep);
+        }
+      } else {
+        auto draw = [&]() {
+          const long long x = (long long)atomicAdd(&hdr->ticket, 1ull);
+          if (x < ntiles) trace_now(kTrTicket, x);
+          return x;
+        };
+        long long t = TK == 0 ? draw() : 0;
+        for (int k = 0;; ++k) {
+          const int s = k % STAGES;
+          if (k >= STAGES) {
+            const uint32_t par = ((k / STAGES) - 1) & 1;
+            if (!mbar_wait_bounded(&empty[s], par, hdr, tmo, (unsigned long long)t)) break;
+            if constexpr (TK == 2) t = draw();
+            pending &= ~(1u << s);
+          } else if constexpr (TK != 0) {
+            t = draw();
+          }
+          *s_tile(s) = t;
+          if (t < ntiles) {
+            issue(s, k, t, pol_l2);
+            if constexpr (TK == 0) t = draw();
+          } else {
+            ptx::mbar_arrive(&full[s]);
+            break;
+          }
         }
       }
       for (int s = 0; s < STAGES; ++s)
         if (pending & (1u << s)) mbar_wait_bounded(&full[s], (pend_par >> s) & 1u, hdr, tmo, 0ull);
     }
     __syncwarp();
+  } else if (CO != 0 && warp == 1) {
+    // ------------------------------------------------------------ carry chain
+    // Scan jobs only; it never touches the stages (a reduce job never waits
+    // for this warp). For the scan jobs of window w: takes the prefix of this
+    // CTA's run from the fold warp, then, tile by tile, fills the next slot of
+    // the ring with the tile's exclusive prefix (the carry chain of the run)
+    // and the segment prefixes of its record. The record of window w's tiles
+    // is complete once the fold warp posts window w's prefix; records are
+    // loaded one tile ahead. Every window is taken (also with an empty run)
+    // so that the fold warp can reuse the window's parity slot.
+    const CoopRuns runs(ntiles, gridDim.x, blockIdx.x, args.coop_kt);
+    const uint64_t* recs = args.desc;
+    constexpr int RW = Cfg::REC_WORDS;
+    constexpr int RCW = Cfg::REC_CW;
+    constexpr size_t RSTRIDE = Cfg::REC_BYTES / 8;
+    constexpr int RL = (RW + 31) / 32;  // this lane's record words: lane, lane + 32, ...
+    auto load_rec = [&](long long t, uint32_t (&rw)[RL]) {
+#pragma unroll
+      for (int q = 0; q < RL; ++q) {
+        const int i = q * 32 + lane;
+        rw[q] = i < RW ? uint32_t(recs[size_t(t) * RSTRIDE + i]) : 0u;
+      }
+    };
+    long long q = 0;  // scan jobs handed out
+    for (long long w = 0; w < runs.R; ++w) {
+      if (!mbar_wait_bounded(&co_winb[w & 1], uint32_t(w >> 1) & 1u, hdr, tmo, 0ull)) break;
+      carry_t carry = co_win[w & 1];
+      __threadfence_block();
+      __syncwarp();
+      if (lane == 0) atomicAdd(&co_cnt[1], 1u);
+      long long t0, t1;
+      runs.run(w, t0, t1);
+      uint32_t rw[RL];
+      if (t0 < t1) load_rec(t0, rw);
+      bool ok = true;
+      for (long long t = t0; t < t1; ++t, ++q) {
+        const int d = int(q % Cfg::RING);
+        if (q >= Cfg::RING &&
+            !mbar_wait_bounded(&co_rfree[d], uint32_t(q / Cfg::RING - 1) & 1u, hdr, tmo, 0ull)) {
+          ok = false;
+          break;
+        }
+        unsigned char* slot = co_slot(d);
+        uint32_t* sa = reinterpret_cast<uint32_t*>(slot + 16);
+        words<carry_t> tw;
+#pragma unroll
+        for (int qq = 0; qq < RL; ++qq) {
+          const int i = qq * 32 + lane;
+          if (i >= RCW && i < RW) sa[i - RCW] = rw[qq];
+        }
+#pragma unroll
+        for (int i = 0; i < RCW; ++i) tw.w[i] = __shfl_sync(kFullMask, rw[0], i);
+        if (lane == 0) *reinterpret_cast<carry_t*>(slot) = carry;
+        __syncwarp();
+        if (lane == 0) ptx::mbar_arrive(&co_rfull[d]);
+        carry = pol.cop(carry, from_words<carry_t>(tw));
+        if (t + 1 < t1) load_rec(t + 1, rw);
+      }
+      if (!ok) break;
+    }
+  } else if (CO != 0 && warp == NC + 2 + (BS == 2 ? 1 : 0)) {
+    // ------------------------------------------------------------ window barriers
+    // Window w in turn: first the prefix of window w - 1 (wait for barrier
+    // w - 1, fold the run aggregates of window w - 1 in block order: this
+    // CTA's run prefix for warp 1), then the run aggregate of window w (once
+    // this CTA's reduce jobs of window w are done): published in slot w % 4,
+    // arrival at barrier w. Slot reuse: a CTA overwrites slot w % 4 with
+    // window w + 4 only after barrier w + 3, which every CTA reaches after its
+    // fold of window w.
+    const CoopRuns runs(ntiles, gridDim.x, blockIdx.x, args.coop_kt);
+    const long long G = gridDim.x, b = blockIdx.x;
+    carry_t* slots = static_cast<carry_t*>(args.coop_aggs);
+    constexpr int CST = int(16 / sizeof(carry_t)) > 0 ? int(16 / sizeof(carry_t)) : 1;
+    auto cop = [&](const carry_t& x, const carry_t& y) { return pol.cop(x, y); };
+    carry_t wcarry = pol.cid();  // all windows before the next one to fold
+    unsigned nred = 0;           // this CTA's reduce jobs up to the current window
+    for (long long w = 0; w <= runs.R; ++w) {
+      if (w >= 1) {
+        const long long v = w - 1;
+        if (!coop_wait_arrivals(hdr, &hdr->coop_arrive[v & 1], (unsigned long long)(v / 2 + 1) * G, tmo,
+                                (unsigned long long)v, lane))
+          break;
+        // all slots of the window at once, FU per lane per round trip
+        constexpr int FU = 8;
+        carry_t pref = pol.cid(), tot = pol.cid();
+        for (long long cc = 0; cc < G; cc += 32 * FU) {
+          carry_t vv[FU];
+#pragma unroll
+          for (int u = 0; u < FU; ++u) {
+            const long long i = cc + u * 32 + lane;
+            vv[u] = i < G ? coop_load_slot(slots + ((v & 3) * G + i) * CST) : pol.cid();
+          }
+#pragma unroll
+          for (int u = 0; u < FU; ++u) {
+            const carry_t inc = warp_inclusive_scan(vv[u], cop, lane);
+            const long long j = b - (cc + u * 32);  // warp-uniform
+            const carry_t before = shfl_idx(inc, (j >= 1 && j < 32) ? int(j - 1) : 0);
+            if (j >= 1 && j < 32) pref = pol.cop(tot, before);
+            if (j == 0) pref = tot;
+            tot = pol.cop(tot, shfl_idx(inc, 31));
+          }
+        }
+        // the parity slot of window v - 2 is free once warp 1 has taken it
+        if (v >= 2 && !coop_wait_smem_count(hdr, &co_cnt[1], unsigned(v - 1), tmo, (unsigned long long)v, lane))
+          break;
+        if (lane == 0) {
+          co_win[v & 1] = pol.cop(wcarry, pref);
+          ptx::mbar_arrive(&co_winb[v & 1]);
+        }
+        wcarry = pol.cop(wcarry, tot);
+        __syncwarp();
+      }
+      if (w < runs.R) {
+        long long t0, t1;
+        runs.run(w, t0, t1);
+        nred += unsigned(t1 - t0);
+        if (!coop_wait_smem_count(hdr, &co_cnt[0], nred, tmo, (unsigned long long)w, lane)) break;
+        if (lane == 0) {
+          coop_store_slot(slots + ((w & 3) * G + b) * CST, co_wagg[w & 1]);
+          co_wagg[w & 1] = pol.cid();
+          __threadfence();
+          atomicAdd(&hdr->coop_arrive[w & 1], 1ull);
+        }
+        __syncwarp();
+      }
+    }
   } else if (warp == 1) {
     // ------------------------------------------------------------ look-back
     for (int k = 0;; ++k) {
@@ -774,7 +1120,7 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
       if (!mbar_wait_bounded(&scanned[s], par, hdr, tmo, 0ull)) break;
       const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(tile, n, head);
       if (lane == 0) {
-        if (out_vec && g.lo == 0 && g.valid == TILE) {
+        if ((CO == 0 || *s_job(s) != 0u) && out_vec && g.lo == 0 && g.valid == TILE) {
           ptx::bulk_s2g_hint(gout + g.gbase, smem + size_t(s) * Cfg::TILE_BYTES, uint32_t(Cfg::TILE_BYTES), pol_l2);
           ptx::bulk_commit();
           ptx::bulk_wait_read<0>();
@@ -969,7 +1315,28 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
         const acc_t xe = shfl_up(x, 1);
         if (lane < NC) s_aggs(s)[lane] = lane == 0 ? pol.aid() : xe;
         const carry_t agg = pol.to_carry(shfl_idx(x, NC - 1));
-        if (lane == 0) {
+        if constexpr (CO != 0) {
+          // cooperative rounds: the tile's record (segment prefixes, then the
+          // aggregate), the run aggregate of the tile's window, then one more
+          // reduce job done
+          uint64_t* rec = args.desc + size_t(tile) * (Cfg::REC_BYTES / 8);
+          if (lane < NC) {
+            const words<acc_t> aw = to_words(lane == 0 ? pol.aid() : xe);
+#pragma unroll
+            for (int i = 0; i < Cfg::REC_AW; ++i) rec[Cfg::REC_CW + lane * Cfg::REC_AW + i] = aw.w[i];
+          }
+          __syncwarp();
+          if (lane == 0) {
+            const words<carry_t> cw = to_words(agg);
+#pragma unroll
+            for (int i = 0; i < Cfg::REC_CW; ++i) rec[i] = cw.w[i];
+            const int p = int((tile / ((long long)gridDim.x * args.coop_kt)) & 1);
+            co_wagg[p] = pol.cop(co_wagg[p], agg);
+            *s_cnt(s) = 0u;
+            __threadfence_block();
+            atomicAdd(&co_cnt[0], 1u);
+          }
+        } else if (lane == 0) {
           *s_tagg(s) = agg;
           *s_cnt(s) = 0u;
           if (tile != args.debug_skip_tile)
@@ -999,24 +1366,15 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
       return true;
     };
 
-    // the reduce pass runs one tile ahead of the scan pass (row statistics:
-    // info_cur of tile k, info_next of tile k + 1)
-    row_info_t info_cur = RF::id(pol), info_next = RF::id(pol);
-    bool have = reduce_pass(0, info_cur);
-    for (int k = 0; have; ++k) {
-      const bool have_next = reduce_pass(k + 1, info_next);
-      const int s = k % STAGES;
-      // scan pass of use k
-      if constexpr (Trace::kOn)
-        if (w == 0 && lane == 0) trace_now(kTrPWait, *s_tile(s));
-      if (!mbar_wait_bounded(&prefb[s], (k / STAGES) & 1, hdr, tmo, 0ull)) break;
-      const long long tile = *s_tile(s);
-      if (w == 0 && lane == 0) trace_now(kTrSStart, tile);
-      const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(tile, n, head);
-      // exclusive prefix of this warp's segment inside the tile (left by the
-      // reduce pass)
-      const acc_t sx = s_aggs(s)[w];
-      const pre_t pw = pol.prepare(w == 0 ? *s_pref(s) : pol.cop(*s_pref(s), pol.to_carry(sx)));
+    // Exclusive prefix of this warp's segment: the tile prefix combined with
+    // the segment's exclusive prefix inside the tile.
+    auto segment_prefix = [&](const carry_t& tile_pref, const acc_t& sx) -> pre_t {
+      return pol.prepare(w == 0 ? tile_pref : pol.cop(tile_pref, pol.to_carry(sx)));
+    };
+    // Scan pass of the tile in stage s (geometry g) with this warp's segment
+    // prefix pw; rows: this warp's row prefixes are in the stage's metadata,
+    // `info_cur` their statistic.
+    auto scan_pass = [&](int s, const StagedGeom& g, const row_info_t& info_cur, const pre_t& pw) {
       if constexpr (LAY == 2) {
         // rows: each row's prefix inside the segment comes from the reduce
         // pass; a thread-serial chain along the row
@@ -1106,6 +1464,61 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
         }
       }
       }
+    };
+
+    if constexpr (CO != 0) {
+      // Cooperative rounds: a reduce job leaves its tile's record and frees
+      // the stage at once; a scan job takes its tile prefix and this warp's
+      // segment prefix from the next slot of warp 1's ring, then runs the scan
+      // pass alone (rows: after this warp's own row totals).
+      long long q = 0;  // scan jobs taken
+      for (int k = 0;; ++k) {
+        const int s = k % STAGES;
+        if (!mbar_wait_bounded(&full[s], (k / STAGES) & 1, hdr, tmo, 0ull)) break;
+        const long long tile = *s_tile(s);
+        if (tile >= ntiles) break;
+        const StagedGeom g = staged_geom<TILE, V, int(sizeof(in_t))>(tile, n, head);
+        row_info_t info = RF::id(pol);
+        if (*s_job(s) == 0u) {
+          record_segment(s, w, tile, reduce_segment(s, w, g, info));
+          if (lane == 0) ptx::mbar_arrive(BS == 2 ? &scanned[s] : &empty[s]);
+          __syncwarp();
+          continue;
+        }
+        if constexpr (LAY == 2) {
+          (void)reduce_segment(s, w, g, info);  // this warp's row prefixes and statistic
+          __syncwarp();
+        }
+        const int d = int(q % Cfg::RING);
+        if (!mbar_wait_bounded(&co_rfull[d], uint32_t(q / Cfg::RING) & 1u, hdr, tmo, 0ull)) break;
+        const unsigned char* slot = co_slot(d);
+        const pre_t pw = segment_prefix(*reinterpret_cast<const carry_t*>(slot),
+                                        reinterpret_cast<const acc_t*>(slot + 16)[w]);
+        __syncwarp();
+        if (lane == 0) ptx::mbar_arrive(&co_rfree[d]);
+        ++q;
+        scan_pass(s, g, info, pw);
+        __syncwarp();
+        if (lane == 0) ptx::mbar_arrive(BS == 2 ? &scanned[s] : &empty[s]);
+      }
+    } else {
+    // the reduce pass runs one tile ahead of the scan pass (row statistics:
+    // info_cur of tile k, info_next of tile k + 1)
+    row_info_t info_cur = RF::id(pol), info_next = RF::id(pol);
+    bool have = reduce_pass(0, info_cur);
+    for (int k = 0; have; ++k) {
+      const bool have_next = reduce_pass(k + 1, info_next);
+      const int s = k % STAGES;
+      // scan pass of use k
+      if constexpr (Trace::kOn)
+        if (w == 0 && lane == 0) trace_now(kTrPWait, *s_tile(s));
+      if (!mbar_wait_bounded(&prefb[s], (k / STAGES) & 1, hdr, tmo, 0ull)) break;
+      const long long tile = *s_tile(s);
+      if (w == 0 && lane == 0) trace_now(kTrSStart, tile);
+      // the tile prefix from warp 1, this segment's prefix inside the tile
+      // from the reduce pass
+      scan_pass(s, staged_geom<TILE, V, int(sizeof(in_t))>(tile, n, head), info_cur,
+                segment_prefix(*s_pref(s), s_aggs(s)[w]));
       __syncwarp();
       if (lane == 0) {
         if (w == 0) trace_now(kTrSDone, tile);
@@ -1114,10 +1527,11 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1)
       have = have_next;
       info_cur = info_next;
     }
+    }
   }
   if constexpr (BS != 0) ptx::bulk_wait<0>();  // this thread's bulk stores are complete
   __syncthreads();
-  if (threadIdx.x == 0) cta_exit_rearm(hdr, args.desc, uint64_t(ntiles) * codec::W);
+  if (threadIdx.x == 0) cta_exit_rearm(hdr, args.desc, CO != 0 ? 0ull : uint64_t(ntiles) * codec::W);
 }
 
 // ---------------------------------------------------------------------------

@@ -386,15 +386,92 @@ struct CoopTuning {
   static constexpr int CH = 4;
 };
 
+// Workspace of the cooperative scan: the staged kernel keeps one record per
+// tile (its aggregate and segment prefixes) between the two reads of a
+// window; the register-tile kernel needs the header and block slots only.
+template <class Pol>
+inline size_t cooperative_workspace_bytes(uint64_t n, const void* in, const void* out) {
+  if constexpr (16 % sizeof(typename Pol::in_t) == 0) {
+    if (tma_path_ok<Pol>(in, out)) {
+      using Cfg = StagedFor<Pol>;
+      const uint64_t ntiles = (n + uint64_t(staged_head<Pol>(in)) + Cfg::TILE - 1) / Cfg::TILE;
+      return workspace_bytes_for_desc_words(ntiles * (Cfg::REC_BYTES / 8));
+    }
+  }
+  return workspace_bytes_for_desc_words(0);
+}
+
+// Window of the cooperative rounds: about this many input bytes per window
+// (two tiles per CTA with 64-72 KB tiles on 152 SMs). The window being
+// scanned and the one being reduced stay in L2 next to the streaming output;
+// on GB300 2^30-element scans ran fastest with 20 MB windows (5.8 TB/s at
+// 2n bytes), 10 MB windows pay the window barrier twice as often (4.9 TB/s)
+// and 30-60 MB windows lose the second read to L2 misses (5.3-4.7 TB/s).
+constexpr uint64_t kCoopWindowBytes = 20ull << 20;
+
 // grid_ctas: 0 = every block the device holds co-resident; a larger request
 // than that fails with grid_too_large (the reference's perform_check,
-// include/cooperative_groups.hpp:65-76).
+// include/cooperative_groups.hpp:65-76). Element-aligned data of element
+// sizes dividing 16 bytes take the staged kernel in cooperative rounds
+// (window_tiles tiles per CTA per window, 0 = about kCoopWindowBytes per
+// window; l2_keep: evict_last instead of evict_normal for a window's first
+// read, which measured the same); the rest take the register-tile kernel
+// (3n traffic).
 template <class Pol>
 inline Status cooperative_scan(cudaStream_t s, const void* in, void* out, uint64_t n, bool exclusive,
-                               void* user_ws = nullptr, size_t user_ws_bytes = 0, int grid_ctas = 0) {
+                               void* user_ws = nullptr, size_t user_ws_bytes = 0, int grid_ctas = 0,
+                               int window_tiles = 0, int l2_keep = 0) {
   if (n == 0) return Status::ok;
   if (!in || !out) return Status::invalid_arg;
   if (!type_aligned<typename Pol::in_t>(in) || !type_aligned<typename Pol::out_t>(out)) return Status::invalid_arg;
+  if constexpr (16 % sizeof(typename Pol::in_t) == 0) {
+    if (tma_path_ok<Pol>(in, out)) {
+      using Tn = DecoupledTuning<Pol>;
+      using Cfg = StagedCfg<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Tn::LAY, (Tn::BS == 2 ? 1 : 0), 1>;
+      DeviceInfo di;
+      Status st = device_info(di);
+      if (st != Status::ok) return st;
+      auto k = decoupled_staged_kernel<Pol, Tn::NC, Tn::CH, Tn::STAGES, Tn::LBW, Tn::LAY, Tn::TK, Tn::PG, Tn::BS,
+                                       NoTrace, 1>;
+      int bps = 0;
+      st = prepare_kernel(k, Cfg::THREADS, Cfg::SMEM, bps);
+      if (st != Status::ok) return st;
+      const uint64_t max_grid = uint64_t(bps) * di.sm_count;
+      uint64_t grid = max_grid;
+      if (grid_ctas > 0) {
+        if (uint64_t(grid_ctas) > max_grid) return Status::grid_too_large;
+        grid = grid_ctas;
+      } else if (settings().max_ctas.load() > 0 && uint64_t(settings().max_ctas.load()) < grid) {
+        grid = settings().max_ctas.load();
+      }
+      const int head = staged_head<Pol>(in);
+      const uint64_t ntiles = (n + uint64_t(head) + Cfg::TILE - 1) / Cfg::TILE;
+      if (ntiles < grid) grid = ntiles;
+      if (grid > uint64_t(kMaxPartials / 4)) grid = kMaxPartials / 4;  // 4 window slots per CTA
+      uint64_t kt = window_tiles > 0 ? uint64_t(window_tiles)
+                                     : (kCoopWindowBytes + grid * Cfg::TILE_BYTES / 2) / (grid * Cfg::TILE_BYTES);
+      if (kt < 1) kt = 1;
+      Ws w;
+      st = acquire_ws(s, cooperative_workspace_bytes<Pol>(n, in, out), user_ws, user_ws_bytes, w);
+      if (st != Status::ok) return st;
+      ScanArgs a{};
+      a.in = in;
+      a.out = out;
+      a.n = n;
+      a.hdr = w.hdr;
+      a.desc = w.desc;
+      a.timeout_ns = settings().timeout_ns.load();
+      a.debug_skip_tile = -1;
+      a.exclusive = exclusive ? 1 : 0;
+      a.head = head;
+      a.coop_kt = int(kt);
+      a.coop_l2 = l2_keep;
+      a.coop_aggs = w.aux;
+      void* params[] = {&a};
+      return from_cuda(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k), dim3(unsigned(grid)),
+                                                   dim3(Cfg::THREADS), params, Cfg::SMEM, s));
+    }
+  }
   using Tn = CoopTuning<Pol>;
   using Cfg = CoopCfg<Pol, Tn::NC, Tn::CH>;
   DeviceInfo di;

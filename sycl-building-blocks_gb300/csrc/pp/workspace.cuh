@@ -6,7 +6,7 @@
 //                                  epoch, sticky error word, abort flag, grid
 //                                  barrier words.
 //   [4096, 4096 + kAuxBytes)       per-block partials (reduction, cooperative
-//                                  scan block aggregates).
+//                                  scan block and window aggregates).
 //   [4096 + kAuxBytes, ...)        look-back descriptors, desc_words() 64-bit
 //                                  words per tile.
 //
@@ -65,6 +65,9 @@ struct WsHeader {
   //     than 32 predecessors (two or more windows), [3] polls that met a
   //     descriptor whose words carried different tags (half written)
   unsigned long long dbg[4];
+  // cooperative rounds of the staged kernel: arrivals at the window barriers,
+  // window w counted in slot w % 2 (re-armed by the last CTA of a launch)
+  unsigned long long coop_arrive[2];
 };
 
 constexpr size_t kHeaderBytes = 4096;
@@ -214,6 +217,8 @@ __device__ __forceinline__ void cta_exit_rearm(WsHeader* h, uint64_t* desc, uint
   h->ticket = 0ull;
   h->abort = 0u;
   h->bar_count = 0u;
+  h->coop_arrive[0] = 0ull;
+  h->coop_arrive[1] = 0ull;
   __threadfence();
   h->done = 0u;
 }

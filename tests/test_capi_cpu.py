@@ -81,4 +81,11 @@ def test_workspace_size_is_host_only(pp):
 
     with pytest.raises(pp.PPError):
         pp.workspace_size("decoupled", "u32", a + 1, a, n)
-    assert pp.workspace_size("cooperative", "f32", a, a, n) == 4096 + 8192 * 16
+    # cooperative rounds: one record per tile, one 64-bit word per 32-bit word
+    # of the tile aggregate and of the segment prefixes (one per compute warp),
+    # rounded up to 16 bytes (float, uint32: 1 + 16 words; uint64: 2 + 20 * 2)
+    assert pp.workspace_size("cooperative", "f32", a, a, n) == 4096 + 8192 * 16 + -(-n // 18432) * 144
+    assert pp.workspace_size("cooperative", "u32", a, a, n) == 4096 + 8192 * 16 + (n // 16384) * 144
+    assert pp.workspace_size("cooperative", "u64", a, a, n) == 4096 + 8192 * 16 + -(-n // 8960) * 336
+    # element-aligned but not 16-byte aligned: still the staged kernel, grid shifted
+    assert pp.workspace_size("cooperative", "u32", a + 4, a, n) == 4096 + 8192 * 16 + (n // 16384 + 1) * 144
