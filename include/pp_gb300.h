@@ -168,8 +168,15 @@ pp_status pp_workspace_status(pp_stream stream, void* d_workspace);
 pp_status pp_set_timeout_ns(uint64_t ns);
 /* Caps the number of CTAs of persistent launches (0 = occupancy x SMs). */
 pp_status pp_set_max_ctas(int ctas);
+/* Window of the cooperative scan's rounds, in tiles per CTA (0 = windows of
+ * about 20 MB, the fastest on GB300; at most 4096). The input streams through
+ * L2 one window at a time: a window is read from HBM by its reduce pass and
+ * again, from L2, by its scan pass one window later. */
+pp_status pp_set_cooperative_window(int tiles_per_cta);
 /* Fault injection for tests: the tile with this index never publishes its
- * look-back descriptor, so its successors' waits time out (-1 = off). */
+ * look-back descriptor, so its successors' waits time out; in the
+ * cooperative scan the CTA whose run holds it never arrives at that window's
+ * barrier (-1 = off). */
 pp_status pp_debug_set_skip_tile(long long tile);
 /* Descriptor-protocol perturbation for tests (no counterpart in the
  * reference, whose look-back correctness depends on timing,

@@ -427,6 +427,12 @@ pp_status pp_set_max_ctas(int ctas) {
   return PP_OK;
 }
 
+pp_status pp_set_cooperative_window(int tiles_per_cta) {
+  if (tiles_per_cta < 0 || tiles_per_cta > 4096) return PP_ERR_INVALID_ARG;
+  pp::host::settings().coop_window_tiles.store(tiles_per_cta);
+  return PP_OK;
+}
+
 pp_status pp_debug_set_skip_tile(long long tile) {
   pp::host::settings().debug_skip_tile.store(tile < 0 ? -1 : tile);
   return PP_OK;

@@ -924,7 +924,7 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0) + (CO != 0 ? 1 : 0
         }
       }
       for (int s = 0; s < STAGES; ++s)
-        if (pending & (1u << s)) mbar_wait_bounded(&full[s], (pend_par >> s) & 1u, hdr, tmo, 0ull);
+        if (pending & (1u << s)) mbar_wait_drain(&full[s], (pend_par >> s) & 1u, hdr, tmo);
     }
     __syncwarp();
   } else if (CO != 0 && warp == 1) {
@@ -1044,7 +1044,11 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0) + (CO != 0 ? 1 : 0
         runs.run(w, t0, t1);
         nred += unsigned(t1 - t0);
         if (!coop_wait_smem_count(hdr, &co_cnt[0], nred, tmo, (unsigned long long)w, lane)) break;
-        if (lane == 0) {
+        // fault injection for tests: the CTA whose run holds the skipped tile
+        // never arrives at this window's barrier, so every CTA's wait for it
+        // times out
+        const bool skip = args.debug_skip_tile >= t0 && args.debug_skip_tile < t1;
+        if (lane == 0 && !skip) {
           coop_store_slot(slots + ((w & 3) * G + b) * CST, co_wagg[w & 1]);
           co_wagg[w & 1] = pol.cid();
           __threadfence();

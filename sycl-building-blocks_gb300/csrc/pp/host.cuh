@@ -46,6 +46,7 @@ struct Settings {
   std::atomic<unsigned> debug_delay_ns{0};  // descriptor perturbation knob (0 = off)
   std::atomic<unsigned> debug_seed{0};
   std::atomic<int> max_ctas{0};  // 0 = occupancy x SMs
+  std::atomic<int> coop_window_tiles{0};  // cooperative rounds: tiles per CTA per window (0 = ~20 MB windows)
 };
 inline Settings& settings() {
   static Settings s;
@@ -448,6 +449,7 @@ inline Status cooperative_scan(cudaStream_t s, const void* in, void* out, uint64
       const uint64_t ntiles = (n + uint64_t(head) + Cfg::TILE - 1) / Cfg::TILE;
       if (ntiles < grid) grid = ntiles;
       if (grid > uint64_t(kMaxPartials / 4)) grid = kMaxPartials / 4;  // 4 window slots per CTA
+      if (window_tiles <= 0) window_tiles = settings().coop_window_tiles.load();
       uint64_t kt = window_tiles > 0 ? uint64_t(window_tiles)
                                      : (kCoopWindowBytes + grid * Cfg::TILE_BYTES / 2) / (grid * Cfg::TILE_BYTES);
       if (kt < 1) kt = 1;
@@ -461,7 +463,7 @@ inline Status cooperative_scan(cudaStream_t s, const void* in, void* out, uint64
       a.hdr = w.hdr;
       a.desc = w.desc;
       a.timeout_ns = settings().timeout_ns.load();
-      a.debug_skip_tile = -1;
+      a.debug_skip_tile = settings().debug_skip_tile.load();
       a.exclusive = exclusive ? 1 : 0;
       a.head = head;
       a.coop_kt = int(kt);

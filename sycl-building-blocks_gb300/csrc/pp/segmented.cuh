@@ -273,7 +273,7 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
         }
       }
       for (int s = 0; s < STAGES; ++s)
-        if (pending & (1u << s)) mbar_wait_bounded(&full[s], (pend_par >> s) & 1u, hdr, tmo, 0ull);
+        if (pending & (1u << s)) mbar_wait_drain(&full[s], (pend_par >> s) & 1u, hdr, tmo);
     }
     __syncwarp();
   } else if (warp == 1) {

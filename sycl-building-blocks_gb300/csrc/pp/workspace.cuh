@@ -196,6 +196,21 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   }
 }
 
+// Wait for this CTA's own bulk copy into a stage before the CTA exits. The
+// abort flag does not end it (the copy must land before the shared memory is
+// released); the time limit does, after recording a timeout.
+__device__ __forceinline__ bool mbar_wait_drain(uint64_t* bar, uint32_t parity, WsHeader* h, uint64_t timeout_ns) {
+  if (ptx::mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = ptx::globaltimer_ns();
+  for (uint32_t it = 1;; ++it) {
+    if (ptx::mbar_try_wait(bar, parity)) return true;
+    if ((it & 15u) == 0u && ptx::globaltimer_ns() - t0 > timeout_ns) {
+      raise_error(h, kDevTimeout, ~0ull);
+      return false;
+    }
+  }
+}
+
 // Called by thread 0 of every CTA after the CTA's last access to the shared
 // control words. The last CTA to exit re-arms the workspace for the next
 // launch on the same stream: ticket and exit counters to zero, abort cleared,

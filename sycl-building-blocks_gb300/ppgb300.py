@@ -48,7 +48,7 @@ EXPORTS = [
     "pp_decoupled_scan_host", "pp_cooperative_scan_host", "pp_scan_host", "pp_reduce_host", "pp_status_string",
     "pp_stream_status", "pp_workspace_status", "pp_set_timeout_ns", "pp_set_max_ctas", "pp_debug_set_skip_tile",
     "pp_version", "pp_decoupled_scan_device_noalloc", "pp_segmented_scan", "pp_segmented_reduce", "pp_rows_scan",
-    "pp_debug_set_lookback_delay", "pp_debug_lookback_counters",
+    "pp_debug_set_lookback_delay", "pp_debug_lookback_counters", "pp_set_cooperative_window",
 ]
 
 
@@ -91,6 +91,7 @@ def lib() -> C.CDLL:
     L.pp_workspace_status.argtypes = [vp, vp]
     L.pp_set_timeout_ns.argtypes = [u64]
     L.pp_set_max_ctas.argtypes = [i32]
+    L.pp_set_cooperative_window.argtypes = [i32]
     L.pp_debug_set_skip_tile.argtypes = [C.c_longlong]
     L.pp_debug_set_lookback_delay.argtypes = [C.c_uint32, C.c_uint32]
     L.pp_debug_lookback_counters.argtypes = [vp, C.POINTER(C.c_uint64)]
@@ -268,6 +269,11 @@ def set_timeout_ns(ns: int) -> None:
 
 def set_max_ctas(ctas: int) -> None:
     _check(lib().pp_set_max_ctas(ctas), "pp_set_max_ctas")
+
+
+def set_cooperative_window(tiles_per_cta: int) -> None:
+    """Tiles per CTA per window of the cooperative scan's rounds (0 = default)."""
+    _check(lib().pp_set_cooperative_window(tiles_per_cta), "pp_set_cooperative_window")
 
 
 def debug_set_skip_tile(tile: int) -> None:

@@ -50,6 +50,9 @@ def test_host_side_argument_checks(pp):
     assert L.pp_reduce_device(None, 0, 1, dummy, 10, None) == pp.PP_ERR_INVALID_ARG
     assert L.pp_set_timeout_ns(0) == pp.PP_ERR_INVALID_ARG
     assert L.pp_set_max_ctas(-1) == pp.PP_ERR_INVALID_ARG
+    assert L.pp_set_cooperative_window(-1) == pp.PP_ERR_INVALID_ARG
+    assert L.pp_set_cooperative_window(4097) == pp.PP_ERR_INVALID_ARG
+    assert L.pp_set_cooperative_window(0) == pp.PP_OK
     assert L.pp_decoupled_scan_host(0, 0, 9, dummy, dummy, 5) == pp.PP_ERR_INVALID_ARG
     # pointers not aligned to the element size
     assert L.pp_scan(None, 0, 0, 1, dummy + 2, dummy, 10, 0, 0) == pp.PP_ERR_INVALID_ARG
