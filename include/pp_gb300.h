@@ -210,7 +210,9 @@ const char* pp_version(void);
  * 2,104,492,029 floats, 511,508,479 elements of an 8-byte integer type or
  * 460,357,631 doubles; larger n returns PP_ERR_WORKSPACE. All calls share the
  * array: calls that overlap on the GPU race, so order them on one stream.
- * The first call on each device looks up the array's address. A device-side
+ * The first call on each device looks up the array's address (once, with
+ * that device current); make that first call before any stream capture on
+ * the device. A device-side
  * timeout of a call stays in the array until pp_stream_status() on the calls'
  * stream returns it. */
 pp_status pp_decoupled_scan_device_noalloc(pp_stream stream, pp_scan_kind kind, pp_op op, pp_dtype dtype,

@@ -29,7 +29,8 @@
 //     threads without ordering) race on the array and give wrong results:
 //     order them on one stream;
 //   * the first call on each device looks up the array's device address with
-//     cudaGetSymbolAddress (once per device, with that device current);
+//     cudaGetSymbolAddress (once per device, with that device current), so
+//     that first call belongs before any stream capture on the device;
 //   * a device-side timeout is recorded in the array's error word, which the
 //     next call leaves alone; pp_stream_status() on the stream of the calls
 //     returns it (and clears it) after the stream's own workspace errors.
