@@ -26,11 +26,10 @@
 // tile reduces on its own, with tile-local prefixes only. The element that
 // ends a non-empty segment whose head lies in the same tile writes the
 // segment's total to rank_out[base + count - 1] (base: the non-empty segments
-// that start before the tile, from a binary search over the offsets; count:
-// the heads of the tile up to the element), a store with no load in front of
-// it. The one segment per tile that was open where the tile begins and ends
-// inside it leaves its piece in the tile's record, beside the tile's
-// aggregate; segment_fixup_kernel scans the records in tile order and
+// that start before the tile, written by the rank pre-pass; count: the heads
+// of the tile up to the element). The one segment per tile that was open
+// where the tile begins and ends inside it leaves its piece in the tile's
+// record, beside the tile's aggregate; segment_fixup_kernel scans the records in tile order and
 // completes those segments, and segment_gather_kernel moves the totals from
 // rank order to their segments (empty segments get the identity from the
 // pre-pass). In the rows layout the data is read once: the reduce pass
@@ -484,6 +483,7 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
         // over the segment is done here, and each row's exclusive prefix stays
         // for the scan pass
         const int r0 = w * Cfg::SEG + lane * (CH * V);
+        bool plain_rows = false;  // no lane's row holds a head: every count is zero
         if constexpr (REDUCE) {
           // the only pass over the data: a chunk holding segment ends leaves
           // the row's running value in place of its elements (the stage is
@@ -492,29 +492,42 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
           unsigned char* stage = smem + size_t(s) * Cfg::TILE_BYTES;
           uint32_t epk = 0;
           const uint32_t hpk = row_bits(s, r0, base, valid, epk);
+          // no head and no end in any lane's whole row (one vote instead of
+          // one per chunk): plain combines, and nothing to leave in the stage
+          if (SKIP && !__any_sync(kFullMask, (hpk | epk) != 0u)) {
+            plain_rows = true;
 #pragma unroll
-          for (int c = 0; c < CH; ++c) {
-            const int e0 = r0 + c * V;
-            in_t x[V];
-            load_row_vals(s, e0, base, valid, bulk, x);
-            const uint32_t hb = (hpk >> (c * V)) & ((1u << V) - 1u);
-            const uint32_t en = (epk >> (c * V)) & ((1u << V) - 1u);
-            if (!SKIP || __any_sync(kFullMask, (hb | en) != 0u)) {
-              union {
-                vec_t u;
-                out_t v[V];
-              } o;
-#pragma unroll
-              for (int j = 0; j < V; ++j) {
-                r = pol.aop(r, pol.load(x[j], (hb >> j) & 1u));
-                o.v[j] = r.v;
-              }
-              if (en) *reinterpret_cast<vec_t*>(stage + size_t(e0) * sizeof(in_t)) = o.u;
-            } else {
-              // no head and no end in any of the warp's chunks: the same
-              // combines with those bits known to be zero
+            for (int c = 0; c < CH; ++c) {
+              in_t x[V];
+              load_row_vals(s, r0 + c * V, base, valid, bulk, x);
 #pragma unroll
               for (int j = 0; j < V; ++j) r = pol.aop(r, pol.load(x[j], false));
+            }
+          } else {
+#pragma unroll
+            for (int c = 0; c < CH; ++c) {
+              const int e0 = r0 + c * V;
+              in_t x[V];
+              load_row_vals(s, e0, base, valid, bulk, x);
+              const uint32_t hb = (hpk >> (c * V)) & ((1u << V) - 1u);
+              const uint32_t en = (epk >> (c * V)) & ((1u << V) - 1u);
+              if (!SKIP || __any_sync(kFullMask, (hb | en) != 0u)) {
+                union {
+                  vec_t u;
+                  out_t v[V];
+                } o;
+#pragma unroll
+                for (int j = 0; j < V; ++j) {
+                  r = pol.aop(r, pol.load(x[j], (hb >> j) & 1u));
+                  o.v[j] = r.v;
+                }
+                if (en) *reinterpret_cast<vec_t*>(stage + size_t(e0) * sizeof(in_t)) = o.u;
+              } else {
+                // no head and no end in any of the warp's chunks: the same
+                // combines with those bits known to be zero
+#pragma unroll
+                for (int j = 0; j < V; ++j) r = pol.aop(r, pol.load(x[j], false));
+              }
             }
           }
           row_heads = hpk;
@@ -531,7 +544,8 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
             for (int j = 0; j < V; ++j) r = pol.aop(r, pol.load(x[j], (hb >> j) & 1u));
           }
         }
-        const acc_t inc = warp_inclusive_scan(r, aop, lane);
+        const acc_t inc = plain_rows ? acc_t{warp_inclusive_scan(r.v, pol.op, lane), 0u}
+                                     : warp_inclusive_scan(r, aop, lane);
         const acc_t ex = shfl_up(inc, 1);
         s_rows(s)[w * 32 + lane] = lane == 0 ? pol.aid() : ex;
         r = shfl_idx(inc, 31);
