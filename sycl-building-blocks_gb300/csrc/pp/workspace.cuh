@@ -178,6 +178,11 @@ __device__ __forceinline__ bool aborted(WsHeader* h) {
   return ptx::ld_relaxed(reinterpret_cast<const uint32_t*>(&h->abort)) != 0u;
 }
 
+// A wait looks at the abort flag (a global load) only once it has lasted this
+// long: the short waits of a healthy pipeline never leave shared memory, and
+// a failure elsewhere still ends every wait within microseconds.
+constexpr uint64_t kAbortCheckAfterNs = 20000;
+
 // Bounded wait on an mbarrier phase. Returns false (after raising a timeout)
 // when the phase has not completed within timeout_ns or another CTA aborted.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, WsHeader* h,
@@ -187,8 +192,9 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   for (uint32_t it = 1;; ++it) {
     if (ptx::mbar_try_wait(bar, parity)) return true;
     if ((it & 15u) == 0u) {
-      if (aborted(h)) return false;
-      if (ptx::globaltimer_ns() - t0 > timeout_ns) {
+      const uint64_t waited = ptx::globaltimer_ns() - t0;
+      if (waited > kAbortCheckAfterNs && aborted(h)) return false;
+      if (waited > timeout_ns) {
         raise_error(h, kDevTimeout, detail);
         return false;
       }
