@@ -62,11 +62,12 @@ __device__ __forceinline__ bool grid_barrier(WsHeader* h, uint64_t timeout_ns) {
       uint32_t it = 0;
       while (ptx::ld_acquire(reinterpret_cast<const uint32_t*>(&h->bar_gen)) == gen) {
         if ((++it & 15u) == 0u) {
-          if (aborted(h)) {
+          const uint64_t waited = ptx::globaltimer_ns() - t0;
+          if (waited > kAbortCheckAfterNs && aborted(h)) {
             ok = 0;
             break;
           }
-          if (ptx::globaltimer_ns() - t0 > timeout_ns) {
+          if (waited > timeout_ns) {
             raise_error(h, kDevTimeout, ~0ull);
             ok = 0;
             break;

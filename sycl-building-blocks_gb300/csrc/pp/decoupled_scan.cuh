@@ -152,9 +152,10 @@ __device__ __forceinline__ bool lookback_warp(const Pol& pol, const uint64_t* de
       if ((spins & 7u) == 0u) {
         bool give_up = false;
         if (lane == 0) {
-          if (aborted(hdr)) {
+          const uint64_t waited = ptx::globaltimer_ns() - t0;
+          if (waited > kAbortCheckAfterNs && aborted(hdr)) {
             give_up = true;
-          } else if (ptx::globaltimer_ns() - t0 > timeout_ns) {
+          } else if (waited > timeout_ns) {
             raise_error(hdr, kDevTimeout, (unsigned long long)tile);
             give_up = true;
           }
@@ -455,9 +456,10 @@ __device__ __forceinline__ bool lookback_multi(const Pol& pol, const uint64_t* d
       if ((spins & 7u) == 0u) {
         bool give_up = false;
         if (lane == 0) {
-          if (aborted(hdr)) {
+          const uint64_t waited = ptx::globaltimer_ns() - t0;
+          if (waited > kAbortCheckAfterNs && aborted(hdr)) {
             give_up = true;
-          } else if (ptx::globaltimer_ns() - t0 > timeout_ns) {
+          } else if (waited > timeout_ns) {
             raise_error(hdr, kDevTimeout, (unsigned long long)tile);
             give_up = true;
           }
@@ -577,9 +579,10 @@ __device__ __forceinline__ bool lookback_pipelined(const Pol& pol, const uint64_
     if ((spins & 7u) != 0u) return true;
     bool give_up = false;
     if (lane == 0) {
-      if (aborted(hdr)) {
+      const uint64_t waited = ptx::globaltimer_ns() - t0;
+      if (waited > kAbortCheckAfterNs && aborted(hdr)) {
         give_up = true;
-      } else if (ptx::globaltimer_ns() - t0 > timeout_ns) {
+      } else if (waited > timeout_ns) {
         raise_error(hdr, kDevTimeout, (unsigned long long)tile);
         give_up = true;
       }
@@ -711,9 +714,10 @@ __device__ __forceinline__ bool coop_wait_arrivals(WsHeader* h, const unsigned l
     if ((it & 15u) == 15u) {
       int stop = 0;
       if (lane == 0) {
-        if (aborted(h)) {
+        const uint64_t waited = ptx::globaltimer_ns() - t0;
+        if (waited > kAbortCheckAfterNs && aborted(h)) {
           stop = 1;
-        } else if (ptx::globaltimer_ns() - t0 > timeout_ns) {
+        } else if (waited > timeout_ns) {
           raise_error(h, kDevTimeout, detail);
           stop = 1;
         }
@@ -740,9 +744,10 @@ __device__ __forceinline__ bool coop_wait_smem_count(WsHeader* h, const unsigned
     if ((it & 15u) == 15u) {
       int stop = 0;
       if (lane == 0) {
-        if (aborted(h)) {
+        const uint64_t waited = ptx::globaltimer_ns() - t0;
+        if (waited > kAbortCheckAfterNs && aborted(h)) {
           stop = 1;
-        } else if (ptx::globaltimer_ns() - t0 > timeout_ns) {
+        } else if (waited > timeout_ns) {
           raise_error(h, kDevTimeout, detail);
           stop = 1;
         }
