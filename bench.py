@@ -277,13 +277,12 @@ def run_ours(args) -> dict | None:
     # pinned host buffers of the end-to-end leg, allocated and filled now: the
     # timed host-array calls made right after pinning 8 GiB met host stalls
     # of 40-130 ms in their first steps.
-    # The first pinned allocations of a process on the GB300 machine (a virtual
-    # machine) get the host pages that earlier processes freed last, and DMA
-    # over those pages meets periodic stalls: 30-200 ms about every 0.5 s,
-    # measured with the same pipeline over buffers pinned first (stalls) and
-    # second (none) in one process, alternating call by call. A pinned guard
-    # allocation taken first and held through the end-to-end leg keeps the
-    # timed buffers off those pages.
+    # On some GB300 machines (virtual machines) DMA over the first pinned
+    # allocations of a process met periodic stalls: 30-200 ms about every
+    # 0.5 s, measured with the same pipeline over buffers pinned first
+    # (stalls) and second (none) in one process, alternating call by call.
+    # A pinned guard allocation taken first and held through the end-to-end
+    # leg keeps the timed buffers out of the first allocations.
     guard = torch.empty(E2E_GUARD_BYTES, dtype=torch.uint8, pin_memory=True)
     h_in = torch.empty(n, dtype=torch.int32, pin_memory=True)
     h_out = torch.empty(n, dtype=torch.int32, pin_memory=True)
@@ -422,8 +421,8 @@ def run_ours(args) -> dict | None:
             "api": "pp_decoupled_scan_host (pinned host buffers; streamed in 64 MiB chunks, both copy directions overlapping the scans)",
             "verified_tail": e2e_ok,
             "host_link_gbs_this_run": link,
-            "host_buffers": "torch pinned (cudaHostAlloc), allocated after a 16 GiB pinned guard: pages freed last by "
-                            "earlier processes meet periodic DMA stalls on this virtual machine",
+            "host_buffers": "torch pinned (cudaHostAlloc), allocated after a 16 GiB pinned guard: the first pinned "
+                            "allocations of a process met periodic DMA stalls on some of these virtual machines",
             "step_ms": e2e_step_ms,
             "warmup_call_ms": warm_ms,
         },
