@@ -54,7 +54,7 @@ class nd_range_barrier {
         mask[g >> 5] |= 1u << (g & 31);
       }
     }
-    return create(s, grid, block, groups, mask, timeout_ns, nullptr, 0);
+    return create(s, block, groups, mask, timeout_ns, nullptr, 0);
   }
 
   // Groups g with predicate(g) true cooperate.
@@ -65,7 +65,7 @@ class nd_range_barrier {
     std::vector<uint32_t> mask(words_for(groups), 0u);
     for (uint64_t g = 0; g < groups; ++g)
       if (predicate(size_t(g))) mask[g >> 5] |= 1u << (g & 31);
-    return create(s, grid, block, groups, mask, timeout_ns, nullptr, 0);
+    return create(s, block, groups, mask, timeout_ns, nullptr, 0);
   }
 
   // As make_barrier, with the co-residency check made against the occupancy
@@ -85,7 +85,7 @@ class nd_range_barrier {
         mask[g >> 5] |= 1u << (g & 31);
       }
     }
-    return create(s, grid, block, groups, mask, timeout_ns, reinterpret_cast<const void*>(kernel), dynamic_smem);
+    return create(s, block, groups, mask, timeout_ns, reinterpret_cast<const void*>(kernel), dynamic_smem);
   }
 
   static void destroy(nd_range_barrier* b) {
@@ -159,7 +159,7 @@ class nd_range_barrier {
   }
 #endif
 
-  static nd_range_barrier* create(cudaStream_t s, dim3 grid, dim3 block, uint64_t groups,
+  static nd_range_barrier* create(cudaStream_t s, dim3 block, uint64_t groups,
                                   const std::vector<uint32_t>& mask, uint64_t timeout_ns, const void* kernel,
                                   size_t dynamic_smem) {
     int dev = 0;
