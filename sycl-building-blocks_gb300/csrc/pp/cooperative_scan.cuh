@@ -134,6 +134,8 @@ __global__ void __launch_bounds__(NC * 32) cooperative_scan_kernel(const CoopArg
   __shared__ carry_t s_carry;
 
   const ScanArgs& args = cargs.s;
+  // the workspace epoch at the start, for the exit re-arm (read early, used last)
+  const uint32_t epoch0 = ptx::ld_relaxed(reinterpret_cast<const uint32_t*>(&args.hdr->epoch));
   const Pol pol{};
   const int cw = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -239,7 +241,7 @@ __global__ void __launch_bounds__(NC * 32) cooperative_scan_kernel(const CoopArg
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) cta_exit_rearm(args.hdr, args.desc, 0);
+  if (threadIdx.x == 0) cta_exit_rearm(args.hdr, args.desc, 0, epoch0);
 }
 
 }  // namespace pp

@@ -1540,7 +1540,7 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0) + (CO != 0 ? 1 : 0
   }
   if constexpr (BS != 0) ptx::bulk_wait<0>();  // this thread's bulk stores are complete
   __syncthreads();
-  if (threadIdx.x == 0) cta_exit_rearm(hdr, args.desc, CO != 0 ? 0ull : uint64_t(ntiles) * codec::W);
+  if (threadIdx.x == 0) cta_exit_rearm(hdr, args.desc, CO != 0 ? 0ull : uint64_t(ntiles) * codec::W, etag - 1u);
 }
 
 // ---------------------------------------------------------------------------
@@ -1635,7 +1635,7 @@ __global__ void __launch_bounds__(NC * 32) decoupled_generic_kernel(const ScanAr
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) cta_exit_rearm(hdr, args.desc, uint64_t(ntiles) * TS::codec::W);
+  if (threadIdx.x == 0) cta_exit_rearm(hdr, args.desc, uint64_t(ntiles) * TS::codec::W, etag - 1u);
 }
 
 }  // namespace pp

@@ -788,7 +788,7 @@ __global__ void __launch_bounds__((NC + 2 + (BS == 2 ? 1 : 0)) * 32, 1) segmente
   }
   if constexpr (BS == 2) ptx::bulk_wait<0>();  // this thread's bulk stores are complete
   __syncthreads();
-  if (threadIdx.x == 0) cta_exit_rearm(hdr, args.desc, uint64_t(ntiles) * codec::W);
+  if (threadIdx.x == 0) cta_exit_rearm(hdr, args.desc, uint64_t(ntiles) * codec::W, etag - 1u);
 }
 
 // ---------------------------------------------------------------------------
