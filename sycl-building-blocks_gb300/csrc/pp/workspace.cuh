@@ -221,21 +221,20 @@ __device__ __forceinline__ bool mbar_wait_drain(uint64_t* bar, uint32_t parity, 
 // control words, with the workspace epoch the launch read when it started.
 // The last CTA to exit re-arms the workspace for the next launch on the same
 // stream: ticket and exit counters to zero, abort cleared, epoch advanced
-// (clearing all descriptors when the epoch wraps). The kernel's end makes
-// these stores visible to the next launch, so the last CTA's path holds no
-// load and no fence besides the exit count's atomic; only the launch whose
-// epoch wraps fences every CTA's descriptor writes before the count, so that
-// the clear comes after all of them.
+// (clearing all descriptors when the epoch wraps). The fences around the exit
+// count order every CTA's counter updates (window arrivals, abort) before the
+// re-arm's stores; the re-arm itself loads nothing (the epoch is the one the
+// launch started with, the descriptor high-water mark grows by a reduction),
+// so the last CTA waits for one atomic and two fences only.
 __device__ __forceinline__ void cta_exit_rearm(WsHeader* h, uint64_t* desc, uint64_t desc_words_used,
                                                uint32_t epoch) {
-  const bool wraps = epoch + 1 >= kEpochLimit;
-  if (wraps) __threadfence();
+  __threadfence();
   const unsigned prev = atomicAdd(&h->done, 1u);
   if (prev != gridDim.x - 1) return;
+  __threadfence();
   if (desc_words_used) atomicMax(&h->desc_words_hwm, (unsigned long long)desc_words_used);
   uint32_t next = epoch + 1;
-  if (wraps) {
-    __threadfence();
+  if (next >= kEpochLimit) {
     const unsigned long long hwm = *reinterpret_cast<volatile unsigned long long*>(&h->desc_words_hwm);
     for (unsigned long long i = 0; i < hwm; ++i) desc[i] = 0ull;
     next = 0;
